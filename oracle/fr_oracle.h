@@ -1,0 +1,110 @@
+/*
+ * fr_oracle.h -- CPU oracle for the fastrecon gridding/recon path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * CPU algorithm (pengwg/fastrecon, ReconData/GridLut.cpp, ReconData/ConvKernel.cpp,
+ * ReconData/ReconData.cpp, ImageFilter/ImageFilter.cpp).  It is used by the
+ * tests as the checker, by __graft_entry__.smoke() as the checker and by
+ * bench.py as the timed CPU baseline.  The product library never links,
+ * loads or calls it.
+ *
+ * Parity pin: the restatement is checked bit-for-bit against the reference's
+ * own CPU sources compiled in oracle/ref_shim (oracle/_ref/libfastrecon_ref.so)
+ * and against fixtures generated from that build (tests/golden/).
+ *
+ * Data layouts (all identical to the reference's in-memory layouts):
+ *   traj   : Point<float>{x[4]} per sample, 16 bytes, sample-major (ReconData.h:12-15)
+ *   dcf    : float per sample
+ *   kdata  : channel-major, each channel N complex64 (re, im interleaved)
+ *   grid   : channel-major, each channel G^d complex64, x fastest (GridLut.cpp:224)
+ */
+#ifndef FR_ORACLE_H
+#define FR_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Modified Bessel function I0 in double precision (power series,
+ * Abramowitz & Stegun 9.6.12).  Stand-in for GSL gsl_sf_bessel_I0, which the
+ * reference calls at ConvKernel.cpp:23.  NaN in -> NaN out. */
+double orc_bessel_i0(double x);
+
+/* Kaiser-Bessel radial LUT, ConvKernel::ConvKernel (ConvKernel.cpp:7-30),
+ * same float/double mix as the reference.  Returns 0 on success. */
+int orc_kb_lut(float kWidth, float overGridFactor, int length, float *out);
+
+/* Per-component bounds as ReconData::loadTraj accumulates them
+ * (ReconData.cpp:159-167).  lo/hi have dim entries. */
+void orc_comp_bounds(const float *traj, size_t n, int dim, float *lo, float *hi);
+
+/* ReconData::normalizeTraj + transformLocalTraj (ReconData.cpp:201-225):
+ * tr = -lo[0], s = (G-1)/(hi[0]-lo[0]) in float; x <- (x + tr) * s for every
+ * component < dim.  lo/hi are updated in place like m_bounds. */
+void orc_normalize_traj(float *traj, size_t n, int dim, unsigned G, float *lo, float *hi,
+                        float *tr_out, float *scale_out);
+
+/* Per-sample clamped cell range, GridLut::griddingChannel (GridLut.cpp:98-106).
+ * start/end are n*3 ints; components >= dim are 0/0 like the reference's
+ * zero-initialised arrays.  Non-finite centres yield an empty range
+ * (start > end), which is what the reference's x86 build produces. */
+void orc_sample_range(const float *traj, size_t n, int dim, unsigned G, float kHW,
+                      int *start, int *end);
+
+/* LUT index the reference uses for one tap (GridLut.cpp:131-136), or -1 if
+ * the tap is outside the kernel radius. */
+int orc_tap_lut_index(float dx, float dy, float dz, float kHW, int klength);
+
+/* One channel of GridLut::griddingChannel (GridLut.cpp:80-147), FP32,
+ * sequential in sample order.  out is G^d complex, overwritten. */
+void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, size_t n,
+                      int dim, unsigned G, float kWidth, const float *lut, int klength,
+                      float *out);
+
+/* GridLut::execute (GridLut.cpp:53-78): all channels, OpenMP over channels
+ * with `threads` threads.  out is channels*G^d complex. */
+void orc_grid(const float *traj, const float *dcf, const float *kdata, size_t n,
+              int channels, int dim, unsigned G, float kWidth, const float *lut,
+              int klength, float *out, int threads);
+
+/* FP64 gridding oracle: same geometry and LUT index as the reference, weights
+ * and accumulation in double.  out is G^d complex double. */
+void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdata, size_t n,
+                          int dim, unsigned G, float kWidth, const float *lut, int klength,
+                          double *out);
+
+/* Tiles touched by each sample for a tile shape (tx,ty,tz): fills, per
+ * sample, lo/hi tile coordinates (n*3 each).  Empty samples get lo > hi on
+ * axis 0.  Used to check the device bin lists bit-for-bit. */
+void orc_sample_tiles(const int *start, const int *end, size_t n, int dim,
+                      const int *tile_shape, int *tlo, int *thi);
+
+/* In-place d-dimensional complex FFT of `batch` contiguous arrays, x fastest,
+ * unnormalised, e^{sign*2*pi*i*k*n/N} (sign=+1 is FFTW_BACKWARD /
+ * CUFFT_INVERSE as used at FFT.cpp:45-47 and cuFFT.cpp:33).  Mixed radix,
+ * computed in double.  Stand-in for FFTW3f, absent on this system. */
+int orc_fft(float *data, int dim, const unsigned *size, int batch, int sign, int threads);
+
+/* ImageFilter::fftShift2 / fftShift3 (ImageFilter.cpp:231-280): the
+ * reference's swap sequence, exactly (also for odd sizes). */
+void orc_fft_shift(float *data, int dim, const unsigned *size);
+
+/* ImageFilter::SOS(reconSize) (ImageFilter.cpp:159-209): centred crop with
+ * offset (size-recon)/2, sum over channels of x*conj(x) in complex float in
+ * channel order, then complex sqrt.  out is recon-size complex. */
+void orc_sos(const float *imgs, int channels, int dim, const unsigned *size,
+             const unsigned *recon, float *out);
+
+/* The whole reference pipeline (Program/Main.cpp:101-181) without I/O:
+ * normalizeTraj, grid, backward FFT, fftShift, SOS, |.| -> float image.
+ * traj is modified in place (as the reference does).  Returns 0 on success. */
+int orc_recon(float *traj, const float *dcf, const float *kdata, size_t n, int channels,
+              int dim, unsigned reconSize, float os, float kWidth, int klength,
+              const unsigned *recon, float *out_mag, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FR_ORACLE_H */

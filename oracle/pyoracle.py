@@ -1,0 +1,203 @@
+"""ctypes bindings to the CPU oracle (test infrastructure only).
+
+``Oracle`` wraps ``oracle/_build/liboracle.so`` (the plain-C restatement of
+the reference CPU path); ``RefLib`` wraps ``oracle/_ref/libfastrecon_ref.so``
+(the reference's own CPU sources compiled against stub headers), present
+only where the reference checkout was available at build time.
+
+Only tests, ``__graft_entry__.smoke`` and ``bench.py``'s CPU-baseline leg use
+this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle as _b
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+
+def cells_of(dim: int, G: int) -> int:
+    return G ** 3 if dim == 3 else G ** 2
+
+
+class Oracle:
+    """The plain-C restatement (fr_oracle.c)."""
+
+    def __init__(self, path: str | None = None):
+        path = path or _b.build_oracle()
+        lib = C.CDLL(path)
+        self.lib = lib
+        lib.orc_bessel_i0.restype = C.c_double
+        lib.orc_bessel_i0.argtypes = [C.c_double]
+        lib.orc_kb_lut.argtypes = [C.c_float, C.c_float, C.c_int, _f32p]
+        lib.orc_comp_bounds.argtypes = [_f32p, C.c_size_t, C.c_int, _f32p, _f32p]
+        lib.orc_normalize_traj.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, _f32p, _f32p,
+                                           C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.orc_sample_range.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _i32p, _i32p]
+        lib.orc_tap_lut_index.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+        lib.orc_grid_channel.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_uint,
+                                         C.c_float, _f32p, C.c_int, _f32p]
+        lib.orc_grid.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_int, C.c_uint,
+                                 C.c_float, _f32p, C.c_int, _f32p, C.c_int]
+        lib.orc_grid_channel_f64.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_uint,
+                                             C.c_float, _f32p, C.c_int, _f64p]
+        lib.orc_sample_tiles.argtypes = [_i32p, _i32p, C.c_size_t, C.c_int, _i32p, _i32p, _i32p]
+        lib.orc_fft.argtypes = [_f32p, C.c_int, _u32p, C.c_int, C.c_int, C.c_int]
+        lib.orc_fft_shift.argtypes = [_f32p, C.c_int, _u32p]
+        lib.orc_sos.argtypes = [_f32p, C.c_int, C.c_int, _u32p, _u32p, _f32p]
+        lib.orc_recon.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_int, C.c_uint,
+                                  C.c_float, C.c_float, C.c_int, _u32p, _f32p, C.c_int]
+
+    # -- ConvKernel --------------------------------------------------------
+    def kb_lut(self, W: float, os_: float, L: int) -> np.ndarray:
+        out = np.zeros(L, np.float32)
+        assert self.lib.orc_kb_lut(W, os_, L, out) == 0
+        return out
+
+    # -- ReconData ---------------------------------------------------------
+    def comp_bounds(self, traj4: np.ndarray, dim: int):
+        lo = np.zeros(3, np.float32)
+        hi = np.zeros(3, np.float32)
+        self.lib.orc_comp_bounds(np.ascontiguousarray(traj4, np.float32), traj4.shape[0], dim, lo, hi)
+        return lo[:dim].copy(), hi[:dim].copy()
+
+    def normalize_traj(self, traj4: np.ndarray, dim: int, G: int):
+        t = np.array(traj4, np.float32, copy=True, order="C")
+        lo = np.zeros(3, np.float32)
+        hi = np.zeros(3, np.float32)
+        self.lib.orc_comp_bounds(t, t.shape[0], dim, lo, hi)
+        tr = C.c_float()
+        sc = C.c_float()
+        self.lib.orc_normalize_traj(t, t.shape[0], dim, G, lo, hi, C.byref(tr), C.byref(sc))
+        return t, np.float32(tr.value), np.float32(sc.value), lo[:dim].copy(), hi[:dim].copy()
+
+    # -- GridLut -----------------------------------------------------------
+    def sample_range(self, traj_norm4: np.ndarray, dim: int, G: int, kHW: float):
+        n = traj_norm4.shape[0]
+        s = np.zeros(n * 3, np.int32)
+        e = np.zeros(n * 3, np.int32)
+        self.lib.orc_sample_range(np.ascontiguousarray(traj_norm4, np.float32), n, dim, G, kHW, s, e)
+        return s.reshape(n, 3), e.reshape(n, 3)
+
+    def sample_tiles(self, start: np.ndarray, end: np.ndarray, dim: int, tile_shape):
+        n = start.shape[0]
+        lo = np.zeros(n * 3, np.int32)
+        hi = np.zeros(n * 3, np.int32)
+        ts = np.array(list(tile_shape) + [1] * (3 - len(tile_shape)), np.int32)
+        self.lib.orc_sample_tiles(np.ascontiguousarray(start, np.int32).ravel(),
+                                  np.ascontiguousarray(end, np.int32).ravel(), n, dim, ts, lo, hi)
+        return lo.reshape(n, 3), hi.reshape(n, 3)
+
+    def grid(self, traj_norm4, dcf, kdata, dim, G, W, lut, threads=1) -> np.ndarray:
+        """kdata: (C, N) complex64; returns (C, G^d) complex64."""
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        Cn, n = kd.shape
+        out = np.zeros((Cn, cells_of(dim, G)), np.complex64)
+        self.lib.orc_grid(np.ascontiguousarray(traj_norm4, np.float32), np.ascontiguousarray(dcf, np.float32),
+                          kd.view(np.float32).ravel(), n, Cn, dim, G, W, np.ascontiguousarray(lut, np.float32),
+                          len(lut), out.view(np.float32).ravel(), threads)
+        return out
+
+    def grid_f64(self, traj_norm4, dcf, kdata, dim, G, W, lut) -> np.ndarray:
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        Cn, n = kd.shape
+        out = np.zeros((Cn, cells_of(dim, G)), np.complex128)
+        for c in range(Cn):
+            o = np.zeros(cells_of(dim, G) * 2, np.float64)
+            self.lib.orc_grid_channel_f64(np.ascontiguousarray(traj_norm4, np.float32),
+                                          np.ascontiguousarray(dcf, np.float32),
+                                          np.ascontiguousarray(kd[c]).view(np.float32), n, dim, G, W,
+                                          np.ascontiguousarray(lut, np.float32), len(lut), o)
+            out[c] = o.view(np.complex128)
+        return out
+
+    # -- ImageFilter -------------------------------------------------------
+    def fft(self, imgs: np.ndarray, dim: int, G: int, sign: int = +1, threads: int = 1) -> np.ndarray:
+        a = np.array(imgs, np.complex64, copy=True, order="C")
+        batch = a.shape[0] if a.ndim > 1 else 1
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        self.lib.orc_fft(a.view(np.float32).ravel(), dim, size, batch, sign, threads)
+        return a
+
+    def fft_shift(self, img: np.ndarray, dim: int, G: int) -> np.ndarray:
+        a = np.array(img, np.complex64, copy=True, order="C")
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        self.lib.orc_fft_shift(a.view(np.float32).ravel(), dim, size)
+        return a
+
+    def sos(self, imgs: np.ndarray, dim: int, G: int, recon) -> np.ndarray:
+        a = np.ascontiguousarray(imgs, np.complex64)
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.complex64)
+        self.lib.orc_sos(a.view(np.float32).ravel(), a.shape[0], dim, size, rec, out.view(np.float32))
+        return out
+
+    def recon(self, traj4, dcf, kdata, dim, reconSize, os_, W, L, recon, threads=1) -> np.ndarray:
+        t = np.array(traj4, np.float32, copy=True, order="C")
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.float32)
+        rc = self.lib.orc_recon(t, np.ascontiguousarray(dcf, np.float32), kd.view(np.float32).ravel(),
+                                t.shape[0], kd.shape[0], dim, reconSize, os_, W, L, rec, out, threads)
+        assert rc == 0
+        return out
+
+
+class RefLib:
+    """The reference's own CPU sources, compiled with stub headers."""
+
+    def __init__(self, path: str | None = None):
+        path = path or _b.ref_lib_path()
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib = C.CDLL(path)
+        self.lib = lib
+        lib.ref_kb_lut.argtypes = [C.c_float, C.c_float, C.c_int, _f32p]
+        lib.ref_grid.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                 C.c_float, C.c_float, C.c_uint, C.c_int, _f32p, _f32p]
+        lib.ref_shift_sos.argtypes = [_f32p, C.c_int, C.c_int, C.c_uint, _u32p, _f32p]
+        lib.ref_recon.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                  C.c_float, C.c_float, C.c_uint, C.c_int, _u32p, _f32p]
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(_b.ref_lib_path())
+
+    def kb_lut(self, W, os_, L):
+        out = np.zeros(L, np.float32)
+        self.lib.ref_kb_lut(W, os_, L, out)
+        return out
+
+    def grid(self, traj4, dcf, kdata, samples, acquisitions, dim, reconSize, os_, W, L, threads=1):
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        G = int(np.float32(reconSize) * np.float32(os_))
+        out = np.zeros((kd.shape[0], cells_of(dim, G)), np.complex64)
+        tn = np.zeros((traj4.shape[0], 4), np.float32)
+        self.lib.ref_grid(np.ascontiguousarray(traj4, np.float32), np.ascontiguousarray(dcf, np.float32),
+                          kd.view(np.float32).ravel(), samples, acquisitions, dim, kd.shape[0], reconSize,
+                          os_, W, L, threads, out.view(np.float32).ravel(), tn)
+        return out, tn
+
+    def shift_sos(self, imgs, dim, G, recon):
+        a = np.ascontiguousarray(imgs, np.complex64)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.complex64)
+        self.lib.ref_shift_sos(a.view(np.float32).ravel(), a.shape[0], dim, G, rec, out.view(np.float32))
+        return out
+
+    def recon(self, traj4, dcf, kdata, samples, acquisitions, dim, reconSize, os_, W, L, recon, threads=1):
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.float32)
+        self.lib.ref_recon(np.ascontiguousarray(traj4, np.float32), np.ascontiguousarray(dcf, np.float32),
+                           kd.view(np.float32).ravel(), samples, acquisitions, dim, kd.shape[0], reconSize,
+                           os_, W, L, threads, rec, out)
+        return out
