@@ -1,0 +1,378 @@
+// fr_capi.cpp -- the C ABI of libfastrecon_gb300.so (include/fastrecon_gb300.h).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "fr_internal.h"
+
+namespace fr {
+
+static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int fail(int status, const std::string &msg)
+{
+    g_last_error = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return FR_ERR_OUT_OF_MEMORY;
+    return FR_ERR_CUDA;
+}
+
+DevBuf::~DevBuf() { release(); }
+
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+int DevBuf::reserve(size_t n)
+{
+    if (n <= bytes && ptr) return 0;
+    release();
+    size_t want = std::max<size_t>(n, 256);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        cuda_fail(e, "cudaMalloc");
+        return 1;
+    }
+    bytes = want;
+    return 0;
+}
+
+// Modified Bessel I0 by its power series (Abramowitz & Stegun 9.6.12);
+// the reference calls GSL's gsl_sf_bessel_I0 (ConvKernel.cpp:23).
+static double bessel_i0(double x)
+{
+    if (std::isnan(x)) return x;
+    double q = 0.25 * x * x, term = 1.0, sum = 1.0;
+    for (int k = 1; k < 1000; ++k) {
+        term *= q / ((double)k * (double)k);
+        sum += term;
+        if (term < sum * 1e-18) break;
+    }
+    return sum;
+}
+
+}  // namespace fr
+
+fr_plan_s::~fr_plan_s()
+{
+    for (auto e : prof_ev) cudaEventDestroy(e);
+}
+
+using namespace fr;
+
+extern "C" {
+
+const char *fr_status_string(int status)
+{
+    switch (status) {
+    case FR_OK: return "ok";
+    case FR_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FR_ERR_SIZE_MISMATCH: return "size mismatch";
+    case FR_ERR_OUT_OF_MEMORY: return "out of memory";
+    case FR_ERR_CUDA: return "CUDA error";
+    case FR_ERR_CUFFT: return "cuFFT error";
+    case FR_ERR_NOT_PLANNED: return "not planned";
+    case FR_ERR_UNSUPPORTED: return "unsupported";
+    case FR_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case FR_ERR_CAPACITY: return "capacity exceeded";
+    }
+    return "unknown status";
+}
+
+const char *fr_last_error(void) { return g_last_error.c_str(); }
+
+const char *fr_version(void) { return "fastrecon_gb300 0.1 (sm_103a)"; }
+
+// ConvKernel::ConvKernel (ConvKernel.cpp:7-30): the same float/double mix.
+int fr_kb_lut(float kWidth, float overGridFactor, int length, float *out)
+{
+    if (length < 2 || !out) return fail(FR_ERR_INVALID_ARGUMENT, "lut length must be >= 2");
+    float w = kWidth, a = overGridFactor;
+    float wa = w * w / (a * a);
+    float beta = (float)(M_PI * std::sqrt((double)wa * ((double)a - 0.5) * ((double)a - 0.5) - 0.8));
+    float dk = (float)((double)w / 2.0 / (double)(length - 1));
+    volatile float kernel0 = 1;  // volatile: keep the float rounding of each step
+    for (int i = 0; i < length; i++) {
+        volatile float k = dk * (float)i;
+        volatile float r = 2 * k / w;
+        double x = (double)beta * std::sqrt(1 - (double)r * (double)r);
+        out[i] = (float)(bessel_i0(x) / (double)w);
+        if (i == 0) kernel0 = out[0];
+        out[i] = out[i] / kernel0;
+    }
+    return FR_OK;
+}
+
+int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
+{
+    if (!d || !out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (d->dim != 2 && d->dim != 3) return fail(FR_ERR_INVALID_ARGUMENT, "dim must be 2 or 3");
+    if (d->grid_size < 1 || d->grid_size > 4096) return fail(FR_ERR_UNSUPPORTED, "grid size must be in [1, 4096]");
+    if (!(d->kernel_width > 0.f) || d->kernel_width > 16.f)
+        return fail(FR_ERR_UNSUPPORTED, "kernel width must be in (0, 16]");
+    if (d->lut_length < 2 || d->lut_length > 16384 || !d->lut)
+        return fail(FR_ERR_INVALID_ARGUMENT, "lut must have 2..16384 entries");
+    auto p = new (std::nothrow) fr_plan_s;
+    if (!p) return fail(FR_ERR_OUT_OF_MEMORY, "plan");
+    cudaGetDevice(&p->device);
+    p->dim = d->dim;
+    p->G = d->grid_size;
+    p->W = d->kernel_width;
+    p->hw = d->kernel_width / 2;  // GridLut.cpp:86: float kHW = width / 2
+    p->L = d->lut_length;
+    p->lut.assign(d->lut, d->lut + d->lut_length);
+    p->flags = d->flags;
+    int tile[3] = {d->tile[0], d->tile[1], d->tile[2]};
+    int cg = d->coil_group;
+    int deft[3];
+    default_tiling(p->dim, deft, &cg, 16);
+    for (int i = 0; i < 3; ++i)
+        if (tile[i] <= 0) tile[i] = deft[i];
+    if (p->dim == 2) tile[2] = 1;
+    if (cg != 4 && cg != 8 && cg != 16 && cg != 32) {
+        delete p;
+        return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");
+    }
+    long long K = (long long)tile[0] * tile[1] * tile[2];
+    int R = floats_per_cell(cg);
+    size_t smem = (size_t)K * R * 4 + (size_t)p->L * 4;
+    if (smem > 227 * 1024) {
+        delete p;
+        return fail(FR_ERR_UNSUPPORTED, "tile x coil group does not fit in shared memory");
+    }
+    if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1 || tile[0] % (32 / std::min(R, 32)) != 0) {
+        delete p;
+        return fail(FR_ERR_UNSUPPORTED, "tile x extent must be a multiple of 32 / floats per cell");
+    }
+    p->coil_group = cg;
+    p->ntiles = 1;
+    for (int i = 0; i < 3; ++i) {
+        p->tile[i] = tile[i];
+        unsigned gi = (i < p->dim) ? p->G : 1u;
+        p->ntile[i] = (int)((gi + tile[i] - 1) / tile[i]);
+        p->ntiles *= p->ntile[i];
+    }
+    if (p->ntiles > (1ll << 30)) {
+        delete p;
+        return fail(FR_ERR_UNSUPPORTED, "too many tiles");
+    }
+    p->chunk = d->chunk > 0 ? d->chunk : 4096;
+    if (p->lut_d.reserve((size_t)p->L * 4)) {
+        delete p;
+        return FR_ERR_OUT_OF_MEMORY;
+    }
+    cudaError_t e = cudaMemcpy(p->lut_d.ptr, p->lut.data(), (size_t)p->L * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "lut upload");
+    }
+    *out = p;
+    return FR_OK;
+}
+
+int fr_plan_destroy(fr_plan p)
+{
+    delete p;
+    return FR_OK;
+}
+
+int fr_plan_set_trajectory(fr_plan p, const float *d_traj, size_t n, void *stream)
+{
+    if (!p || (!d_traj && n)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return plan_run(p, d_traj, n, (cudaStream_t)stream);
+}
+
+int fr_plan_normalized_trajectory(fr_plan p, float *d_out, void *stream)
+{
+    if (!p || !d_out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "no trajectory");
+    if (p->n == 0) return FR_OK;
+    FR_CUDA(cudaMemcpyAsync(d_out, p->traj.ptr, p->n * 16, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return FR_OK;
+}
+
+int fr_plan_bounds(fr_plan p, float *raw_lo, float *raw_hi, float *norm_lo, float *norm_hi)
+{
+    if (!p) return fail(FR_ERR_INVALID_ARGUMENT, "null plan");
+    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "no trajectory");
+    for (int i = 0; i < 3; ++i) {
+        if (raw_lo) raw_lo[i] = p->bounds_host[i];
+        if (raw_hi) raw_hi[i] = p->bounds_host[3 + i];
+        if (norm_lo) norm_lo[i] = p->bounds_host[6 + i];
+        if (norm_hi) norm_hi[i] = p->bounds_host[9 + i];
+    }
+    return FR_OK;
+}
+
+int fr_plan_sample_ranges(fr_plan p, int *d_start, int *d_end, void *stream)
+{
+    if (!p || !d_start || !d_end) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "no trajectory");
+    return sample_ranges_run(p, d_start, d_end, (cudaStream_t)stream);
+}
+
+int fr_plan_stats(fr_plan p, long long *tiles, long long *pairs, long long *items, long long *slots)
+{
+    if (!p) return fail(FR_ERR_INVALID_ARGUMENT, "null plan");
+    if (tiles) *tiles = p->ntiles;
+    if (pairs) *pairs = p->npairs;
+    if (items) *items = p->nitems;
+    if (slots) *slots = p->nslots;
+    return FR_OK;
+}
+
+int fr_plan_bins(fr_plan p, long long *d_tile_offset, unsigned *d_pairs, void *stream)
+{
+    if (!p || !d_tile_offset || !d_pairs) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "no trajectory");
+    cudaStream_t s = (cudaStream_t)stream;
+    // tile offsets are the .pairs field of the exclusive TileScan
+    FR_CUDA(cudaMemcpy2DAsync(d_tile_offset, sizeof(long long), p->tile_scan.ptr, sizeof(TileScan),
+                              sizeof(long long), (size_t)p->ntiles + 1, cudaMemcpyDeviceToDevice, s));
+    if (p->npairs)
+        FR_CUDA(cudaMemcpyAsync(d_pairs, p->pairs.ptr, (size_t)p->npairs * 4, cudaMemcpyDeviceToDevice, s));
+    return FR_OK;
+}
+
+int fr_plan_profile(fr_plan p, int enable)
+{
+    if (!p) return fail(FR_ERR_INVALID_ARGUMENT, "null plan");
+    p->profile = enable != 0;
+    p->prof_used = 0;
+    return FR_OK;
+}
+
+int fr_plan_profile_read(fr_plan p, double *ms, int *launches)
+{
+    if (!p) return fail(FR_ERR_INVALID_ARGUMENT, "null plan");
+    double total = 0;
+    if (p->prof_used > 0) FR_CUDA(cudaEventSynchronize(p->prof_ev[p->prof_used * 2 - 1]));
+    for (int i = 0; i < p->prof_used; ++i) {
+        float t = 0;
+        FR_CUDA(cudaEventElapsedTime(&t, p->prof_ev[2 * i], p->prof_ev[2 * i + 1]));
+        total += t;
+    }
+    if (ms) *ms = total;
+    if (launches) *launches = p->prof_used;
+    p->prof_used = 0;
+    return FR_OK;
+}
+
+long long fr_kernel_launches(void) { return g_launches.load(); }
+
+int fr_grid(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid, void *stream)
+{
+    if (!p || !d_grid || (p->n && (!d_kdata || !d_dcf))) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_kdata) & 7) || (reinterpret_cast<uintptr_t>(d_grid) & 7))
+        return fail(FR_ERR_INVALID_ARGUMENT, "complex buffers must be 8-byte aligned");
+    return grid_run(p, d_kdata, d_dcf, channels, d_grid, (cudaStream_t)stream);
+}
+
+// --------------------------------------------------------------------------
+// cuFFT stage
+// --------------------------------------------------------------------------
+
+struct fr_fft_s {
+    cufftHandle h = 0;
+    int sign = CUFFT_INVERSE;
+    size_t elems = 0;
+};
+
+int fr_fft_create(int dim, const unsigned *size, int batch, int sign, fr_fft *out)
+{
+    if (!out || !size || (dim != 2 && dim != 3) || batch < 1)
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad fft arguments");
+    *out = nullptr;
+    auto f = new (std::nothrow) fr_fft_s;
+    if (!f) return fail(FR_ERR_OUT_OF_MEMORY, "fft");
+    // Layout x fastest: cuFFT wants the slowest dimension first.
+    long long n[3];
+    if (dim == 3) {
+        n[0] = size[2];
+        n[1] = size[1];
+        n[2] = size[0];
+    } else {
+        n[0] = size[1];
+        n[1] = size[0];
+    }
+    long long dist = (long long)size[0] * size[1] * (dim == 3 ? size[2] : 1);
+    cufftResult r = cufftCreate(&f->h);
+    size_t work = 0;
+    if (r == CUFFT_SUCCESS)
+        r = cufftMakePlanMany64(f->h, dim, n, nullptr, 1, dist, nullptr, 1, dist, CUFFT_C2C, batch, &work);
+    if (r != CUFFT_SUCCESS) {
+        if (f->h) cufftDestroy(f->h);
+        delete f;
+        return fail(FR_ERR_CUFFT, "cufftMakePlanMany64 failed (" + std::to_string((int)r) + ")");
+    }
+    // FFTW_BACKWARD (+1) == CUFFT_INVERSE (cuImageFilter.cpp:27-31)
+    f->sign = sign > 0 ? CUFFT_INVERSE : CUFFT_FORWARD;
+    f->elems = (size_t)dist * batch;
+    *out = f;
+    return FR_OK;
+}
+
+int fr_fft_execute(fr_fft f, float *d_data, void *stream)
+{
+    if (!f || !d_data) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    cufftResult r = cufftSetStream(f->h, (cudaStream_t)stream);
+    if (r == CUFFT_SUCCESS)
+        r = cufftExecC2C(f->h, reinterpret_cast<cufftComplex *>(d_data), reinterpret_cast<cufftComplex *>(d_data),
+                         f->sign);
+    if (r != CUFFT_SUCCESS) return fail(FR_ERR_CUFFT, "cufftExecC2C failed (" + std::to_string((int)r) + ")");
+    return FR_OK;
+}
+
+int fr_fft_destroy(fr_fft f)
+{
+    if (f) {
+        cufftDestroy(f->h);
+        delete f;
+    }
+    return FR_OK;
+}
+
+int fr_fft_shift(float *d_imgs, int channels, int dim, const unsigned *size, void *stream)
+{
+    if (!d_imgs || !size || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad shift arguments");
+    return shift_run(d_imgs, channels, dim, size, (cudaStream_t)stream);
+}
+
+int fr_crop(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *crop, float *d_out,
+            void *stream)
+{
+    if (!d_imgs || !d_out || !size || !crop || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad crop arguments");
+    return crop_run(d_imgs, channels, dim, size, crop, d_out, (cudaStream_t)stream);
+}
+
+int fr_sos(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *recon,
+           const float *d_deapod, float *d_out, void *stream)
+{
+    if (!d_imgs || !d_out || !size || !recon || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad sos arguments");
+    return sos_run(d_imgs, channels, dim, size, recon, d_deapod, d_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// fr_internal.h -- internal declarations of libfastrecon_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/fastrecon_gb300.h"
+
+namespace fr {
+
+// Thread-local error detail; returns `status` for use in `return fail(...)`.
+int fail(int status, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+void note_launch();
+
+#define FR_CUDA(call)                                   \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return ::fr::cuda_fail(e_, #call); \
+    } while (0)
+
+// Call once after every kernel launch: counts it and checks the launch.
+#define FR_CHECK_LAUNCH(name)                           \
+    do {                                                \
+        ::fr::note_launch();                            \
+        cudaError_t e_ = cudaGetLastError();            \
+        if (e_ != cudaSuccess) return ::fr::cuda_fail(e_, name); \
+    } while (0)
+
+// Device buffer with capacity reuse (cudaMalloc / cudaFree).
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~DevBuf();
+    int reserve(size_t n);  // grows only; contents are not preserved
+    void release();
+    template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// One work item of the scatter: a tile and a chunk of its sorted bin.
+struct WorkItem {
+    long long begin;  // first index into pairs[]
+    int count;        // samples in this chunk
+    int tile;         // tile index (row-major over the tile grid)
+    int slot;         // partial slot for split tiles, -1 otherwise
+    int pad;
+};
+
+// A tile whose bin was split into several work items.
+struct SplitTile {
+    int tile;
+    int first_slot;
+    int nslots;
+    int pad;
+};
+
+// Scan tuple over tiles: pairs, work items, partial slots, split tiles.
+struct TileScan {
+    long long pairs, items, slots, splits;
+};
+
+}  // namespace fr
+
+struct fr_plan_s {
+    int device = 0;
+    int dim = 2;
+    unsigned G = 0;
+    float W = 4.f, hw = 2.f;
+    int L = 0;
+    std::vector<float> lut;
+    int tile[3] = {1, 1, 1};
+    int ntile[3] = {1, 1, 1};
+    long long ntiles = 0;
+    int coil_group = 8;
+    int chunk = 4096;
+    unsigned flags = 0;
+
+    size_t n = 0;
+    bool planned = false;
+    long long npairs = 0, nitems = 0, nslots = 0, nsplits = 0;
+    float bounds_host[12] = {0};  // raw lo[3], raw hi[3], norm lo[3], norm hi[3]
+
+    fr::DevBuf lut_d;         // L floats
+    fr::DevBuf traj;          // n float4, normalised
+    fr::DevBuf bounds;        // 16 floats: raw lo/hi as ordered ints, tr, scale, norm lo/hi
+    fr::DevBuf tile_count;    // ntiles int
+    fr::DevBuf tile_fill;     // ntiles int
+    fr::DevBuf tile_scan;     // (ntiles + 1) TileScan, exclusive
+    fr::DevBuf scan_blocks;   // scan scratch
+    fr::DevBuf pairs;         // npairs uint32
+    fr::DevBuf items;         // nitems WorkItem
+    fr::DevBuf splits;        // nsplits SplitTile
+    fr::DevBuf partials;      // nslots * ngroups * K * R floats
+    fr::DevBuf ranges;        // scratch for fr_plan_sample_ranges (unused otherwise)
+
+    // scatter-kernel timing (fr_plan_profile)
+    bool profile = false;
+    std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
+    int prof_used = 0;
+    ~fr_plan_s();
+};
+
+namespace fr {
+// Kernel-side entry points implemented in the .cu files.
+int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
+int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+             cudaStream_t s);
+int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
+int sos_run(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *recon,
+            const float *d_deapod, float *d_out, cudaStream_t s);
+int shift_run(float *d_imgs, int channels, int dim, const unsigned *size, cudaStream_t s);
+int crop_run(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *crop,
+             float *d_out, cudaStream_t s);
+// Default tile shape / coil group for a configuration.
+void default_tiling(int dim, int *tile, int *coil_group, int channels);
+// Floats per tile cell in shared memory for a coil group.
+int floats_per_cell(int coil_group);
+}  // namespace fr
+
+namespace fr {
+int deapod_seed_run(float *d_grid, int dim, int G, float hw, const float *d_lut, int L, int checkerboard,
+                    cudaStream_t s);
+int deapod_map_run(const float *d_img, int dim, const unsigned *size, const unsigned *recon, float *d_out,
+                   cudaStream_t s);
+}  // namespace fr

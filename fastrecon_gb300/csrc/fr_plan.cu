@@ -1,0 +1,481 @@
+// fr_plan.cu -- trajectory normalisation and tile binning (the plan).
+//
+// Replaces ReconData::normalizeTraj (ReconData.cpp:211-225) and
+// cuGridLut::plan (cuGridLut.cu:151-226).  Instead of materialising one
+// (cell, sample) pair per kernel tap and sorting them, each sample is binned
+// into the grid tiles its clamped cell range touches (at most 2^d tiles when
+// the tile edge is at least the kernel footprint), with an integer counting
+// sort: count per tile, exclusive scan, fill.  The per-sample cell range is
+// the reference's (GridLut.cpp:98-106), computed with the same float
+// operations, so the set of touched tiles is bit-exact.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <limits.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "fr_device.cuh"
+#include "fr_internal.h"
+
+namespace fr {
+namespace {
+
+constexpr int kBoundsSlots = 32;
+// bounds buffer layout (32-bit words)
+constexpr int kRawLoEnc = 0;   // 3 ordered-int encodings
+constexpr int kRawHiEnc = 3;   // 3
+constexpr int kTr = 6;         // float
+constexpr int kScale = 7;      // float
+constexpr int kNormLo = 8;     // 3 floats
+constexpr int kNormHi = 11;    // 3 floats
+constexpr int kRawLo = 14;     // 3 floats (decoded)
+constexpr int kRawHi = 17;     // 3 floats
+
+__device__ __forceinline__ int float_order(float f)
+{
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float order_float(int i)
+{
+    return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF);
+}
+
+__global__ void bounds_init_kernel(int *b)
+{
+    int t = threadIdx.x;
+    if (t < 3) {
+        // ReconData.cpp:158-161: first = max(), second = lowest()
+        b[kRawLoEnc + t] = float_order(FLT_MAX);
+        b[kRawHiEnc + t] = float_order(-FLT_MAX);
+    }
+}
+
+// Component bounds as ReconData::loadTraj accumulates them
+// (ReconData.cpp:167-174): NaN never replaces a bound.
+__global__ void bounds_kernel(const float4 *__restrict__ traj, size_t n, int dim, int *b)
+{
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 p = traj[i];
+        float c[3] = {p.x, p.y, p.z};
+        for (int d = 0; d < 3; ++d) {
+            if (d < dim && !isnan(c[d])) {
+                int o = float_order(c[d]);
+                lo[d] = min(lo[d], o);
+                hi[d] = max(hi[d], o);
+            }
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+            hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int d = 0; d < dim; ++d) {
+            if (lo[d] != INT_MAX) atomicMin(&b[kRawLoEnc + d], lo[d]);
+            if (hi[d] != INT_MIN) atomicMax(&b[kRawHiEnc + d], hi[d]);
+        }
+    }
+}
+
+// ReconData::normalizeTraj (ReconData.cpp:211-225), one thread.
+__global__ void scale_kernel(int *b, int dim, unsigned G)
+{
+    float *f = reinterpret_cast<float *>(b);
+    float lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = d < dim ? order_float(b[kRawLoEnc + d]) : 0.f;
+        hi[d] = d < dim ? order_float(b[kRawHiEnc + d]) : 0.f;
+        f[kRawLo + d] = lo[d];
+        f[kRawHi + d] = hi[d];
+    }
+    float tr = -lo[0];
+    float scale = __fdiv_rn((float)(G - 1u), __fsub_rn(hi[0], lo[0]));
+    f[kTr] = tr;
+    f[kScale] = scale;
+    for (int d = 0; d < 3; ++d) {
+        f[kNormLo + d] = d < dim ? __fmul_rn(__fadd_rn(lo[d], tr), scale) : 0.f;
+        f[kNormHi + d] = d < dim ? __fmul_rn(__fadd_rn(hi[d], tr), scale) : 0.f;
+    }
+}
+
+struct BinGeom {
+    int dim;
+    unsigned G;
+    float hw;
+    int tile[3];
+    int ntile[3];
+};
+
+// Normalise one sample (ReconData.cpp:201-209: (x + tr) * scale) and find
+// the tiles its clamped cell range touches.  Returns the number of tiles;
+// lo/hi receive the tile-coordinate box.
+__device__ __forceinline__ int sample_tiles(const BinGeom &g, float4 &p, int *lo, int *hi)
+{
+    float c[3] = {p.x, p.y, p.z};
+    int cnt = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d < g.dim) {
+            int s, e;
+            comp_range(c[d], g.hw, g.G, s, e);
+            if (s > e) cnt = 0;
+            lo[d] = s / g.tile[d];
+            hi[d] = e / g.tile[d];
+        } else {
+            lo[d] = hi[d] = 0;
+        }
+    }
+    if (cnt) cnt = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+    return cnt;
+}
+
+__device__ __forceinline__ int tile_of(const BinGeom &g, const int *lo, const int *hi, int j)
+{
+    int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
+    int tx = lo[0] + j % nx;
+    int r = j / nx;
+    int ty = lo[1] + r % ny;
+    int tz = lo[2] + r / ny;
+    return (tz * g.ntile[1] + ty) * g.ntile[0] + tx;
+}
+
+// Pass 1: normalise, store the normalised trajectory, count samples per
+// tile.  Counts are aggregated per warp over lanes that hit the same tile
+// (consecutive samples of a readout usually do), so a dense tile sees one
+// atomic per warp instead of one per sample.
+__global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n, BinGeom g,
+                                       const int *__restrict__ b, float4 *__restrict__ out,
+                                       int *__restrict__ tile_count)
+{
+    const float *bf = reinterpret_cast<const float *>(b);
+    const float tr = bf[kTr], scale = bf[kScale];
+    const int lane = threadIdx.x & 31;
+    for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n;
+         base += (size_t)gridDim.x * blockDim.x) {
+        size_t i = base + threadIdx.x;
+        int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
+        int cnt = 0;
+        if (i < n) {
+            float4 p = raw[i];
+            float4 q;
+            q.x = __fmul_rn(__fadd_rn(p.x, tr), scale);
+            q.y = g.dim > 1 ? __fmul_rn(__fadd_rn(p.y, tr), scale) : 0.f;
+            q.z = g.dim > 2 ? __fmul_rn(__fadd_rn(p.z, tr), scale) : 0.f;
+            q.w = 0.f;
+            out[i] = q;
+            cnt = sample_tiles(g, q, lo, hi);
+        }
+        int maxcnt = __reduce_max_sync(0xffffffffu, cnt);
+        for (int j = 0; j < maxcnt; ++j) {
+            bool valid = j < cnt;
+            int t = valid ? tile_of(g, lo, hi, j) : -1 - lane;
+            unsigned m = __match_any_sync(0xffffffffu, t);
+            int leader = __ffs(m) - 1;
+            if (valid && lane == leader) atomicAdd(&tile_count[t], __popc(m));
+        }
+    }
+}
+
+// Pass 3: fill the sorted bin lists.
+__global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g,
+                            const TileScan *__restrict__ scan, int *__restrict__ tile_fill,
+                            unsigned *__restrict__ pairs)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n;
+         base += (size_t)gridDim.x * blockDim.x) {
+        size_t i = base + threadIdx.x;
+        int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
+        int cnt = 0;
+        if (i < n) {
+            float4 q = traj[i];
+            cnt = sample_tiles(g, q, lo, hi);
+        }
+        int maxcnt = __reduce_max_sync(0xffffffffu, cnt);
+        for (int j = 0; j < maxcnt; ++j) {
+            bool valid = j < cnt;
+            int t = valid ? tile_of(g, lo, hi, j) : -1 - lane;
+            unsigned m = __match_any_sync(0xffffffffu, t);
+            int leader = __ffs(m) - 1;
+            int basepos = 0;
+            if (valid && lane == leader) basepos = atomicAdd(&tile_fill[t], __popc(m));
+            basepos = __shfl_sync(0xffffffffu, basepos, leader);
+            if (valid) {
+                long long pos = scan[t].pairs + basepos + __popc(m & lt);
+                pairs[pos] = (unsigned)i;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ TileScan tile_value(int cnt, int chunk)
+{
+    TileScan v;
+    long long items = cnt == 0 ? 1 : (cnt + chunk - 1) / chunk;
+    v.pairs = cnt;
+    v.items = items;
+    v.slots = items > 1 ? items : 0;
+    v.splits = items > 1 ? 1 : 0;
+    return v;
+}
+
+__device__ __forceinline__ TileScan add(const TileScan &a, const TileScan &b)
+{
+    return TileScan{a.pairs + b.pairs, a.items + b.items, a.slots + b.slots, a.splits + b.splits};
+}
+
+__device__ __forceinline__ TileScan shfl_up(const TileScan &v, int d)
+{
+    TileScan r;
+    r.pairs = __shfl_up_sync(0xffffffffu, v.pairs, d);
+    r.items = __shfl_up_sync(0xffffffffu, v.items, d);
+    r.slots = __shfl_up_sync(0xffffffffu, v.slots, d);
+    r.splits = __shfl_up_sync(0xffffffffu, v.splits, d);
+    return r;
+}
+
+constexpr int kScanThreads = 256;
+constexpr int kScanPerThread = 8;
+constexpr int kScanSeg = kScanThreads * kScanPerThread;
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+__device__ TileScan block_exclusive(TileScan v, TileScan *total)
+{
+    __shared__ TileScan warp_tot[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    TileScan inc = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        TileScan o = shfl_up(inc, d);
+        if (lane >= d) inc = add(inc, o);
+    }
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    TileScan wpre{0, 0, 0, 0}, all{0, 0, 0, 0};
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+        if (w < warp) wpre = add(wpre, warp_tot[w]);
+        all = add(all, warp_tot[w]);
+    }
+    __syncthreads();
+    *total = all;
+    TileScan exc = add(wpre, inc);
+    exc.pairs -= v.pairs;
+    exc.items -= v.items;
+    exc.slots -= v.slots;
+    exc.splits -= v.splits;
+    return exc;
+}
+
+__global__ void scan_reduce_kernel(const int *__restrict__ cnt, long long ntiles, int chunk,
+                                   TileScan *__restrict__ block_sums)
+{
+    long long seg0 = (long long)blockIdx.x * kScanSeg;
+    TileScan v{0, 0, 0, 0};
+    for (int k = 0; k < kScanPerThread; ++k) {
+        long long t = seg0 + (long long)k * kScanThreads + threadIdx.x;
+        if (t < ntiles) v = add(v, tile_value(cnt[t], chunk));
+    }
+    TileScan tot;
+    block_exclusive(v, &tot);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// Exclusive scan of the block sums in place (single block, looping).
+__global__ void scan_blocks_kernel(TileScan *sums, int nblocks)
+{
+    __shared__ TileScan carry;
+    if (threadIdx.x == 0) carry = TileScan{0, 0, 0, 0};
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += kScanThreads) {
+        int i = base + threadIdx.x;
+        TileScan v = i < nblocks ? sums[i] : TileScan{0, 0, 0, 0};
+        TileScan tot;
+        TileScan exc = block_exclusive(v, &tot);
+        TileScan c = carry;
+        if (i < nblocks) sums[i] = add(exc, c);
+        __syncthreads();
+        if (threadIdx.x == 0) carry = add(c, tot);
+        __syncthreads();
+    }
+}
+
+__global__ void scan_write_kernel(const int *__restrict__ cnt, long long ntiles, int chunk,
+                                  const TileScan *__restrict__ block_sums, TileScan *__restrict__ out)
+{
+    // Each thread owns kScanPerThread consecutive tiles of the segment.
+    long long seg0 = (long long)blockIdx.x * kScanSeg;
+    long long t0 = seg0 + (long long)threadIdx.x * kScanPerThread;
+    TileScan local[kScanPerThread];
+    TileScan v{0, 0, 0, 0};
+    for (int k = 0; k < kScanPerThread; ++k) {
+        long long t = t0 + k;
+        local[k] = t < ntiles ? tile_value(cnt[t], chunk) : TileScan{0, 0, 0, 0};
+        v = add(v, local[k]);
+    }
+    TileScan tot;
+    TileScan exc = add(block_exclusive(v, &tot), block_sums[blockIdx.x]);
+    for (int k = 0; k < kScanPerThread; ++k) {
+        long long t = t0 + k;
+        if (t < ntiles) out[t] = exc;
+        exc = add(exc, local[k]);
+        if (t == ntiles - 1) out[ntiles] = exc;
+    }
+}
+
+__global__ void items_kernel(const int *__restrict__ cnt, const TileScan *__restrict__ scan,
+                             long long ntiles, int chunk, WorkItem *__restrict__ items,
+                             SplitTile *__restrict__ splits)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntiles;
+         t += (long long)gridDim.x * blockDim.x) {
+        int c = cnt[t];
+        TileScan v = tile_value(c, chunk);
+        TileScan o = scan[t];
+        for (long long k = 0; k < v.items; ++k) {
+            WorkItem w;
+            w.begin = o.pairs + k * chunk;
+            w.count = c == 0 ? 0 : (int)min((long long)chunk, (long long)c - k * chunk);
+            w.tile = (int)t;
+            w.slot = v.items > 1 ? (int)(o.slots + k) : -1;
+            w.pad = 0;
+            items[o.items + k] = w;
+        }
+        if (v.items > 1) {
+            SplitTile s;
+            s.tile = (int)t;
+            s.first_slot = (int)o.slots;
+            s.nslots = (int)v.items;
+            s.pad = 0;
+            splits[o.splits] = s;
+        }
+    }
+}
+
+__global__ void ranges_kernel(const float4 *__restrict__ traj, size_t n, int dim, unsigned G, float hw,
+                              int *__restrict__ start, int *__restrict__ end)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 p = traj[i];
+        float c[3] = {p.x, p.y, p.z};
+        for (int d = 0; d < 3; ++d) {
+            int s = 0, e = 0;
+            if (d < dim) comp_range(c[d], hw, G, s, e);
+            start[3 * i + d] = s;
+            end[3 * i + d] = e;
+        }
+    }
+}
+
+int grid_blocks(size_t n, int threads)
+{
+    size_t b = (n + threads - 1) / threads;
+    return (int)std::max<size_t>(1, std::min<size_t>(b, 152 * 32));
+}
+
+}  // namespace
+
+int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
+{
+    if ((reinterpret_cast<uintptr_t>(d_traj) & 15) != 0)
+        return fail(FR_ERR_INVALID_ARGUMENT, "trajectory pointer must be 16-byte aligned");
+    if (n > 0xFFFFFFFFull) return fail(FR_ERR_UNSUPPORTED, "more than 2^32-1 samples");
+    p->planned = false;
+    p->n = n;
+    if (p->bounds.reserve(kBoundsSlots * 4)) return FR_ERR_OUT_OF_MEMORY;
+    if (p->traj.reserve(std::max<size_t>(n, 1) * 16)) return FR_ERR_OUT_OF_MEMORY;
+    if (p->tile_count.reserve(p->ntiles * 4) || p->tile_fill.reserve(p->ntiles * 4) ||
+        p->tile_scan.reserve((p->ntiles + 1) * sizeof(TileScan)))
+        return FR_ERR_OUT_OF_MEMORY;
+    long long nblocks = (p->ntiles + kScanSeg - 1) / kScanSeg;
+    if (p->scan_blocks.reserve(std::max<long long>(nblocks, 1) * sizeof(TileScan))) return FR_ERR_OUT_OF_MEMORY;
+
+    int *b = p->bounds.as<int>();
+    FR_CUDA(cudaMemsetAsync(p->tile_count.ptr, 0, p->ntiles * 4, s));
+    FR_CUDA(cudaMemsetAsync(p->tile_fill.ptr, 0, p->ntiles * 4, s));
+    bounds_init_kernel<<<1, 32, 0, s>>>(b);
+    FR_CHECK_LAUNCH("bounds_init_kernel");
+    const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
+    if (n > 0) {
+        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, p->dim, b);
+        FR_CHECK_LAUNCH("bounds_kernel");
+    }
+    scale_kernel<<<1, 1, 0, s>>>(b, p->dim, p->G);
+    FR_CHECK_LAUNCH("scale_kernel");
+
+    BinGeom g;
+    g.dim = p->dim;
+    g.G = p->G;
+    g.hw = p->hw;
+    for (int d = 0; d < 3; ++d) {
+        g.tile[d] = p->tile[d];
+        g.ntile[d] = p->ntile[d];
+    }
+    float4 *traj = p->traj.as<float4>();
+    if (n > 0) {
+        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, traj,
+                                                                   p->tile_count.as<int>());
+        FR_CHECK_LAUNCH("normalize_count_kernel");
+    }
+    TileScan *bs = p->scan_blocks.as<TileScan>();
+    TileScan *scan = p->tile_scan.as<TileScan>();
+    scan_reduce_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(p->tile_count.as<int>(), p->ntiles, p->chunk, bs);
+    FR_CHECK_LAUNCH("scan_reduce_kernel");
+    scan_blocks_kernel<<<1, kScanThreads, 0, s>>>(bs, (int)nblocks);
+    FR_CHECK_LAUNCH("scan_blocks_kernel");
+    scan_write_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(p->tile_count.as<int>(), p->ntiles, p->chunk, bs,
+                                                            scan);
+    FR_CHECK_LAUNCH("scan_write_kernel");
+
+    TileScan tot;
+    FR_CUDA(cudaMemcpyAsync(&tot, scan + p->ntiles, sizeof(TileScan), cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaMemcpyAsync(p->bounds_host, reinterpret_cast<float *>(b) + kNormLo, 6 * 4,
+                            cudaMemcpyDeviceToHost, s));
+    float raw_b[6];
+    FR_CUDA(cudaMemcpyAsync(raw_b, reinterpret_cast<float *>(b) + kRawLo, 6 * 4, cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaStreamSynchronize(s));
+    // bounds_host: raw lo[3], raw hi[3], norm lo[3], norm hi[3]
+    float norm_b[6];
+    for (int i = 0; i < 6; ++i) norm_b[i] = p->bounds_host[i];
+    for (int i = 0; i < 6; ++i) p->bounds_host[i] = raw_b[i];
+    for (int i = 0; i < 6; ++i) p->bounds_host[6 + i] = norm_b[i];
+
+    if (tot.pairs > 0xFFFFFFFFll || tot.items > INT_MAX || tot.slots > INT_MAX)
+        return fail(FR_ERR_UNSUPPORTED, "bin lists exceed 32-bit indexing");
+    p->npairs = tot.pairs;
+    p->nitems = tot.items;
+    p->nslots = tot.slots;
+    p->nsplits = tot.splits;
+    if (p->pairs.reserve(std::max<long long>(tot.pairs, 1) * 4) ||
+        p->items.reserve(std::max<long long>(tot.items, 1) * sizeof(WorkItem)) ||
+        p->splits.reserve(std::max<long long>(tot.splits, 1) * sizeof(SplitTile)))
+        return FR_ERR_OUT_OF_MEMORY;
+    if (n > 0) {
+        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, scan, p->tile_fill.as<int>(),
+                                                        p->pairs.as<unsigned>());
+        FR_CHECK_LAUNCH("fill_kernel");
+    }
+    items_kernel<<<grid_blocks(p->ntiles, 256), 256, 0, s>>>(p->tile_count.as<int>(), scan, p->ntiles,
+                                                             p->chunk, p->items.as<WorkItem>(),
+                                                             p->splits.as<SplitTile>());
+    FR_CHECK_LAUNCH("items_kernel");
+    p->planned = true;
+    return FR_OK;
+}
+
+int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s)
+{
+    if (p->n == 0) return FR_OK;
+    ranges_kernel<<<grid_blocks(p->n, 256), 256, 0, s>>>(p->traj.as<float4>(), p->n, p->dim, p->G, p->hw,
+                                                          d_start, d_end);
+    FR_CHECK_LAUNCH("ranges");
+    return FR_OK;
+}
+
+}  // namespace fr

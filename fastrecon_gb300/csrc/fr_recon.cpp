@@ -1,0 +1,199 @@
+// fr_recon.cpp -- the whole reconstruction behind one object
+// (Program/Main.cpp:101-181 without file I/O): normalise + bin the
+// trajectory, grid every coil, backward FFT of all coils in one batched
+// cuFFT call, crop + sum of squares (+ optional deapodization).
+//
+// With an even grid the fftShift of the reference (ImageFilter.cpp:40-53)
+// is folded into the gridding flush as a (-1)^(x+y+z) modulation, so the
+// FFT output is already shifted and no extra pass over the grid is needed.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <new>
+
+#include "fr_internal.h"
+
+using namespace fr;
+
+struct fr_recon_s {
+    fr_recon_desc d;
+    unsigned G = 0;
+    size_t cells = 0;
+    bool checkerboard = false;
+    std::vector<float> lut;
+    fr_plan plan = nullptr;
+    fr_fft fft = nullptr;
+    fr_fft fft1 = nullptr;  // single-image plan for the deapodization map
+    DevBuf grid;            // channels x G^d complex
+    DevBuf deapod;          // out_size floats
+    DevBuf h_traj, h_dcf, h_kdata, h_img;  // device staging for host-buffer runs
+    bool deapod_ready = false;
+    bool timing = false;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    float stage_ms[4] = {-1, -1, -1, -1};
+    ~fr_recon_s()
+    {
+        if (plan) fr_plan_destroy(plan);
+        if (fft) fr_fft_destroy(fft);
+        if (fft1) fr_fft_destroy(fft1);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
+extern "C" {
+
+int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
+{
+    if (!d || !out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (d->dim != 2 && d->dim != 3) return fail(FR_ERR_INVALID_ARGUMENT, "dim must be 2 or 3");
+    if (d->channels < 1) return fail(FR_ERR_INVALID_ARGUMENT, "channels must be positive");
+    auto r = new (std::nothrow) fr_recon_s;
+    if (!r) return fail(FR_ERR_OUT_OF_MEMORY, "recon");
+    r->d = *d;
+    if (d->dim == 2) r->d.out_size[2] = 1;
+    // GridLut.cpp:45: m_gridSize = unsigned(reconSize * overGridFactor)
+    r->G = (unsigned)((float)d->recon_size * d->overgrid_factor);
+    r->cells = d->dim == 3 ? (size_t)r->G * r->G * r->G : (size_t)r->G * r->G;
+    r->checkerboard = (r->G % 2) == 0;
+    r->lut.resize(d->lut_length > 1 ? d->lut_length : 2);
+    int st = fr_kb_lut(d->kernel_width, d->overgrid_factor, d->lut_length, r->lut.data());
+    if (st) {
+        delete r;
+        return st;
+    }
+    fr_plan_desc pd = {};
+    pd.dim = d->dim;
+    pd.grid_size = r->G;
+    pd.kernel_width = d->kernel_width;
+    pd.lut_length = d->lut_length;
+    pd.lut = r->lut.data();
+    for (int i = 0; i < 3; ++i) pd.tile[i] = d->tile[i];
+    pd.coil_group = d->coil_group > 0 ? d->coil_group : 0;
+    if (pd.coil_group == 0) {
+        int cg = 4;
+        while (cg < d->channels && cg < 16) cg <<= 1;
+        pd.coil_group = cg;
+    }
+    pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
+    st = fr_plan_create(&pd, &r->plan);
+    if (!st) {
+        unsigned sz[3] = {r->G, r->G, d->dim == 3 ? r->G : 1u};
+        st = fr_fft_create(d->dim, sz, d->channels, +1, &r->fft);
+    }
+    if (!st && r->grid.reserve(r->cells * 8 * (size_t)d->channels)) st = FR_ERR_OUT_OF_MEMORY;
+    if (st) {
+        delete r;
+        return st;
+    }
+    const char *tm = std::getenv("FR_TIMING");
+    r->timing = tm && tm[0] == '1';
+    if (r->timing)
+        for (auto &e : r->ev) cudaEventCreate(&e);
+    *out = r;
+    return FR_OK;
+}
+
+int fr_recon_destroy(fr_recon r)
+{
+    delete r;
+    return FR_OK;
+}
+
+static int ensure_deapod(fr_recon r, cudaStream_t s)
+{
+    if (r->deapod_ready) return FR_OK;
+    size_t nout = (size_t)r->d.out_size[0] * r->d.out_size[1] * r->d.out_size[2];
+    if (r->deapod.reserve(nout * 4)) return FR_ERR_OUT_OF_MEMORY;
+    if (!r->fft1) {
+        unsigned sz[3] = {r->G, r->G, r->d.dim == 3 ? r->G : 1u};
+        int st = fr_fft_create(r->d.dim, sz, 1, +1, &r->fft1);
+        if (st) return st;
+    }
+    float *g = r->grid.as<float>();
+    int st = deapod_seed_run(g, r->d.dim, (int)r->G, r->d.kernel_width / 2, r->plan->lut_d.as<float>(),
+                             r->d.lut_length, r->checkerboard ? 1 : 0, s);
+    if (!st) st = fr_fft_execute(r->fft1, g, s);
+    unsigned sz[3] = {r->G, r->G, r->d.dim == 3 ? r->G : 1u};
+    if (!st && !r->checkerboard) st = shift_run(g, 1, r->d.dim, sz, s);
+    if (!st) st = deapod_map_run(g, r->d.dim, sz, r->d.out_size, r->deapod.as<float>(), s);
+    if (!st) r->deapod_ready = true;
+    return st;
+}
+
+int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata, size_t n,
+                 float *d_image, void *stream)
+{
+    if (!r || !d_image || (n && (!d_traj || !d_dcf || !d_kdata)))
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = FR_OK;
+    if (r->d.flags & FR_RECON_DEAPODIZE) {
+        st = ensure_deapod(r, s);
+        if (st) return st;
+    }
+    unsigned sz[3] = {r->G, r->G, r->d.dim == 3 ? r->G : 1u};
+    float *g = r->grid.as<float>();
+    if (r->timing) cudaEventRecord(r->ev[0], s);
+    st = fr_plan_set_trajectory(r->plan, d_traj, n, stream);
+    if (r->timing) cudaEventRecord(r->ev[1], s);
+    if (!st) st = fr_grid(r->plan, d_kdata, d_dcf, r->d.channels, g, stream);
+    if (r->timing) cudaEventRecord(r->ev[2], s);
+    if (!st) st = fr_fft_execute(r->fft, g, stream);
+    if (!st && !r->checkerboard) st = shift_run(g, r->d.channels, r->d.dim, sz, s);
+    if (r->timing) cudaEventRecord(r->ev[3], s);
+    if (!st)
+        st = sos_run(g, r->d.channels, r->d.dim, sz, r->d.out_size,
+                     (r->d.flags & FR_RECON_DEAPODIZE) ? r->deapod.as<float>() : nullptr, d_image, s);
+    if (r->timing) {
+        cudaEventRecord(r->ev[4], s);
+        cudaEventSynchronize(r->ev[4]);
+        for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&r->stage_ms[i], r->ev[i], r->ev[i + 1]);
+    }
+    return st;
+}
+
+int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata, size_t n,
+                      float *h_image, void *stream)
+{
+    if (!r || !h_image || (n && (!h_traj || !h_dcf || !h_kdata)))
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (n > r->d.max_samples) return fail(FR_ERR_CAPACITY, "n exceeds max_samples");
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t nout = (size_t)r->d.out_size[0] * r->d.out_size[1] * r->d.out_size[2];
+    size_t cap = r->d.max_samples > 0 ? r->d.max_samples : 1;
+    if (r->h_traj.reserve(cap * 16) || r->h_dcf.reserve(cap * 4) ||
+        r->h_kdata.reserve(cap * 8 * (size_t)r->d.channels) || r->h_img.reserve(nout * 4))
+        return FR_ERR_OUT_OF_MEMORY;
+    if (n) {
+        FR_CUDA(cudaMemcpyAsync(r->h_traj.ptr, h_traj, n * 16, cudaMemcpyHostToDevice, s));
+        FR_CUDA(cudaMemcpyAsync(r->h_dcf.ptr, h_dcf, n * 4, cudaMemcpyHostToDevice, s));
+        FR_CUDA(cudaMemcpyAsync(r->h_kdata.ptr, h_kdata, n * 8 * (size_t)r->d.channels, cudaMemcpyHostToDevice, s));
+    }
+    int st = fr_recon_run(r, r->h_traj.as<float>(), r->h_dcf.as<float>(), r->h_kdata.as<float>(), n,
+                          r->h_img.as<float>(), stream);
+    if (st) return st;
+    FR_CUDA(cudaMemcpyAsync(h_image, r->h_img.ptr, nout * 4, cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaStreamSynchronize(s));
+    return FR_OK;
+}
+
+int fr_recon_plan(fr_recon r, fr_plan *out)
+{
+    if (!r || !out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    *out = r->plan;
+    return FR_OK;
+}
+
+int fr_recon_stage_ms(fr_recon r, float *plan_ms, float *grid_ms, float *fft_ms, float *sos_ms)
+{
+    if (!r) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (plan_ms) *plan_ms = r->stage_ms[0];
+    if (grid_ms) *grid_ms = r->stage_ms[1];
+    if (fft_ms) *fft_ms = r->stage_ms[2];
+    if (sos_ms) *sos_ms = r->stage_ms[3];
+    return FR_OK;
+}
+
+}  // extern "C"

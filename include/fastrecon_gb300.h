@@ -1,0 +1,210 @@
+/*
+ * fastrecon_gb300.h -- C ABI of libfastrecon_gb300.so, the GB300 (sm_103a)
+ * gridding / reconstruction path behind fastrecon's C++ API.
+ *
+ * Every entry point takes plain pointers, sizes and an optional CUDA stream
+ * (passed as `void *`, a cudaStream_t; NULL = the legacy default stream) and
+ * returns an fr_status.  Device pointers are caller-owned; the library only
+ * allocates the internal buffers of the opaque plan objects.  Each entry
+ * point cites the reference (pengwg/fastrecon) interface it replaces.
+ *
+ * Layouts are the reference's in-memory layouts:
+ *   trajectory : Point<float>{x[4]} per sample (16 B, sample-major),
+ *                ReconData/ReconData.h:12-15
+ *   dcf        : float per sample (ReconData.h:59)
+ *   k-space    : channel-major, N complex64 per channel (ReconData.h:58)
+ *   grid/image : channel-major, G^d complex64 per channel, x fastest
+ *                (ImageData/ImageData.h, GridLut.cpp:94,111)
+ * Sizes are (x, y, z) like ImageSize (ImageData/common.h:7-12); z = 1 in 2D.
+ */
+#ifndef FASTRECON_GB300_H
+#define FASTRECON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FR_OK = 0,
+    FR_ERR_INVALID_ARGUMENT = 1, /* bad pointer, dimension or size */
+    FR_ERR_SIZE_MISMATCH = 2,    /* sizes that must agree do not */
+    FR_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+    FR_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    FR_ERR_CUFFT = 5,            /* a cuFFT call failed */
+    FR_ERR_NOT_PLANNED = 6,      /* execute before plan (cuGridLut.cu:31-34) */
+    FR_ERR_UNSUPPORTED = 7,      /* parameter outside the supported range */
+    FR_ERR_DEVICE_TIMEOUT = 8,   /* a bounded device-side wait expired */
+    FR_ERR_CAPACITY = 9          /* a fixed-capacity buffer is too small */
+} fr_status;
+
+/* Text for a status code; never NULL. */
+const char *fr_status_string(int status);
+/* Detail of the last error raised on the calling thread (may be ""). */
+const char *fr_last_error(void);
+/* Library version string. */
+const char *fr_version(void);
+
+/* ------------------------------------------------------------------------
+ * ConvKernel (ReconData/ConvKernel.h:10-14, ConvKernel.cpp:7-30)
+ * Radial Kaiser-Bessel LUT of `length` entries on radius [0, W/2],
+ * Beatty beta, normalised so lut[0] = 1.  Host computation.
+ * ---------------------------------------------------------------------- */
+int fr_kb_lut(float kernel_width, float overgrid_factor, int length, float *lut_host);
+
+/* ------------------------------------------------------------------------
+ * Gridding plan: GridLut::plan + cuGridLut::plan
+ * (ReconData/GridLut.h:20, GridLut.cpp:41-51, cuGridLut.cu:151-226)
+ *
+ * The plan normalises the trajectory exactly like ReconData::normalizeTraj
+ * (ReconData.cpp:211-225: translation -min, scale (G-1)/(max-min) of
+ * component 0, applied to every component), computes each sample's clamped
+ * cell range exactly like GridLut.cpp:98-106, and bins samples into grid
+ * tiles with an integer counting sort.  The input trajectory is not
+ * modified; fr_plan_normalized_trajectory returns the normalised copy.
+ * ---------------------------------------------------------------------- */
+typedef struct fr_plan_s *fr_plan;
+
+enum {
+    FR_PLAN_CHECKERBOARD = 1u << 0 /* multiply grid cell (x,y,z) by (-1)^(x+y+z)
+                                      on output, which makes the backward FFT
+                                      produce the fftShift-ed image (even G) */
+};
+
+typedef struct {
+    int dim;               /* 2 or 3 (ReconData::rcDim) */
+    unsigned grid_size;    /* G = unsigned(reconSize * overGridFactor), GridLut.cpp:45 */
+    float kernel_width;    /* W (full width), ConvKernel kWidth */
+    int lut_length;        /* L, ConvKernel length (512 in Program/Main.cpp:127) */
+    const float *lut;      /* host pointer to the L-entry LUT (fr_kb_lut) */
+    int tile[3];           /* tile shape in cells (x,y,z); 0 = default */
+    int coil_group;        /* coils per scatter pass (4, 8, 16, 32); 0 = default */
+    int chunk;             /* max samples per work item before a tile is split; 0 = default */
+    unsigned flags;        /* FR_PLAN_* */
+} fr_plan_desc;
+
+int fr_plan_create(const fr_plan_desc *desc, fr_plan *out_plan);
+int fr_plan_destroy(fr_plan plan);
+
+/* Bin a trajectory (device pointer, n Point<float> samples, raw k-space
+ * coordinates).  Replaces ReconData::normalizeTraj + cuGridLut::plan.
+ * Synchronises `stream` once (to size the bin lists). */
+int fr_plan_set_trajectory(fr_plan plan, const float *d_traj, size_t n, void *stream);
+
+/* Normalised trajectory (device, n x 4 floats) as ReconData::getTraj would
+ * hold it after plan; component bounds before/after normalisation
+ * (ReconData::getCompBounds, ReconData.h:31-33) as host floats lo[3],hi[3]. */
+int fr_plan_normalized_trajectory(fr_plan plan, float *d_traj_out, void *stream);
+int fr_plan_bounds(fr_plan plan, float *raw_lo, float *raw_hi, float *norm_lo, float *norm_hi);
+
+/* Per-sample clamped cell ranges (device, n x 3 ints each), exactly the
+ * start/end of GridLut.cpp:98-106; components >= dim are 0. */
+int fr_plan_sample_ranges(fr_plan plan, int *d_start, int *d_end, void *stream);
+
+/* Plan statistics: number of tiles, (sample, tile) pairs, work items and
+ * split-tile partial slots.  Host ints. */
+int fr_plan_stats(fr_plan plan, long long *tiles, long long *pairs, long long *items,
+                  long long *partial_slots);
+
+/* Sorted bin lists (device): tile_offset[tiles+1] (int64) and
+ * pairs[pairs] (uint32 sample index), for bit-exact binning checks. */
+int fr_plan_bins(fr_plan plan, long long *d_tile_offset, unsigned *d_pairs, void *stream);
+
+/* Kernel timing (the reference prints per-stage wall times,
+ * cuGridLut.cu:36-45; this is its device-side counterpart).  While enabled,
+ * every fr_grid call records CUDA events on its stream around the tile
+ * scatter kernel alone; fr_plan_profile_read waits for the last one and
+ * returns the summed duration (ms) and launch count, then resets. */
+int fr_plan_profile(fr_plan plan, int enable);
+int fr_plan_profile_read(fr_plan plan, double *scatter_ms, int *launches);
+
+/* Number of kernels this library has launched in the process (its own
+ * kernels; cuFFT's are not counted). */
+long long fr_kernel_launches(void);
+
+/* ------------------------------------------------------------------------
+ * Gridding: cuGridLut::execute / griddingChannel
+ * (cuGridLut.cu:28-48,231-309; CPU oracle GridLut.cpp:80-147)
+ * d_kdata: channels x n complex64; d_dcf: n floats; d_grid: channels x G^d
+ * complex64, fully overwritten (cells no sample touches are written 0).
+ * ---------------------------------------------------------------------- */
+int fr_grid(fr_plan plan, const float *d_kdata, const float *d_dcf, int channels,
+            float *d_grid, void *stream);
+
+/* ------------------------------------------------------------------------
+ * FFT stage: cuFFT::plan / cuFFT::excute (ImageFilter/cuFFT.cpp:15-37),
+ * ImageFilter::fftPlan / fftExecute (ImageFilter.cpp:211-229).
+ * In-place unnormalised C2C transform of `batch` contiguous images;
+ * sign +1 = CUFFT_INVERSE / FFTW_BACKWARD (the reference default).
+ * ---------------------------------------------------------------------- */
+typedef struct fr_fft_s *fr_fft;
+int fr_fft_create(int dim, const unsigned *size, int batch, int sign, fr_fft *out_fft);
+int fr_fft_execute(fr_fft fft, float *d_data, void *stream);
+int fr_fft_destroy(fr_fft fft);
+
+/* ImageFilter::fftShift (ImageFilter.cpp:40-53,231-280) on `channels`
+ * images of `size`, in place, with the reference's swap semantics (also for
+ * odd sizes). */
+int fr_fft_shift(float *d_imgs, int channels, int dim, const unsigned *size, void *stream);
+
+/* ImageFilter::crop (ImageFilter.cpp:120-157): centred crop, offset
+ * (size - crop)/2, of each channel into d_out (channels x crop complex). */
+int fr_crop(const float *d_imgs, int channels, int dim, const unsigned *size,
+            const unsigned *crop, float *d_out, void *stream);
+
+/* ImageFilter::SOS(reconSize) + the |.| of Program/Main.cpp:177-180
+ * (ImageFilter.cpp:159-209): centred crop, sum over channels of re^2+im^2
+ * in channel order, sqrt.  d_out: recon-size floats.  d_deapod (nullable):
+ * recon-size floats the magnitude is divided by (deapodization, absent in
+ * the reference; NULL reproduces the reference). */
+int fr_sos(const float *d_imgs, int channels, int dim, const unsigned *size,
+           const unsigned *recon, const float *d_deapod, float *d_out, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Whole reconstruction (Program/Main.cpp:101-181 without file I/O):
+ * normalise + bin, grid, backward FFT, shift, crop + SoS (+ optional
+ * deapodization), magnitude.
+ * ---------------------------------------------------------------------- */
+typedef struct fr_recon_s *fr_recon;
+
+enum {
+    FR_RECON_DEAPODIZE = 1u << 0 /* divide by the kernel's image-domain apodization */
+};
+
+typedef struct {
+    int dim;                 /* 2 or 3 */
+    unsigned recon_size;     /* rcxres: G = unsigned(recon_size * overgrid_factor) */
+    float overgrid_factor;   /* os */
+    float kernel_width;      /* W */
+    int lut_length;          /* L (512 in Program/Main.cpp:127) */
+    unsigned out_size[3];    /* rcxres, rcyres, rczres (z = 1 in 2D) */
+    int channels;            /* coils */
+    size_t max_samples;      /* capacity for n */
+    int tile[3];             /* 0 = default */
+    int coil_group;          /* 0 = default */
+    unsigned flags;          /* FR_RECON_* */
+} fr_recon_desc;
+
+int fr_recon_create(const fr_recon_desc *desc, fr_recon *out);
+int fr_recon_destroy(fr_recon r);
+/* Device buffers: d_traj n x 4 raw coordinates, d_dcf n, d_kdata channels x n
+ * complex64, d_image out_size floats (|SoS|).  Re-bins the trajectory. */
+int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata,
+                 size_t n, float *d_image, void *stream);
+/* Same with HOST buffers (pinned for full speed): the host->device copies of
+ * the inputs and the device->host copy of the image are part of the call,
+ * which returns once the image is in h_image. */
+int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata,
+                      size_t n, float *h_image, void *stream);
+/* Plan object and grid workspace used by the recon (for stage timing). */
+int fr_recon_plan(fr_recon r, fr_plan *out_plan);
+/* Stage timings of the last fr_recon_run* call in ms (plan, grid, fft, sos),
+ * measured with CUDA events when FR_TIMING=1 in the environment, else -1. */
+int fr_recon_stage_ms(fr_recon r, float *plan_ms, float *grid_ms, float *fft_ms, float *sos_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTRECON_GB300_H */

@@ -250,6 +250,34 @@ void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdat
     }
 }
 
+void orc_sample_mass(const float *traj, size_t n, int dim, unsigned G, float kWidth,
+                     const float *lut, int klength, double *mass, int threads)
+{
+    float kHW = kWidth / 2;
+    if (threads < 1)
+        threads = 1;
+    (void)threads;
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (long long s = 0; s < (long long)n; ++s) {
+        float center[3] = {0, 0, 0};
+        int start[3] = {0, 0, 0}, end[3] = {0, 0, 0};
+        for (int i = 0; i < dim; ++i) {
+            center[i] = traj[4 * s + i];
+            comp_range(center[i], kHW, G, &start[i], &end[i]);
+        }
+        double m = 0;
+        for (int z = start[2]; z <= end[2]; z++)
+            for (int y = start[1]; y <= end[1]; y++)
+                for (int x = start[0]; x <= end[0]; x++) {
+                    int ki = orc_tap_lut_index((float)x - center[0], (float)y - center[1],
+                                               (float)z - center[2], kHW, klength);
+                    if (ki >= 0)
+                        m += (double)lut[ki];
+                }
+        mass[s] = m;
+    }
+}
+
 void orc_sample_tiles(const int *start, const int *end, size_t n, int dim,
                       const int *tile_shape, int *tlo, int *thi)
 {

@@ -75,6 +75,13 @@ void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdat
                           int dim, unsigned G, float kWidth, const float *lut, int klength,
                           double *out);
 
+/* Per-sample kernel mass: sum over the sample's valid taps of lut[ki], with
+ * the reference geometry (GridLut.cpp:98-136), in double.  Gridding is
+ * linear, so sum_cells grid[c] = sum_s dcf[s]*kdata[c][s]*mass[s]: a
+ * size-independent checksum for full-size runs.  OpenMP over samples. */
+void orc_sample_mass(const float *traj, size_t n, int dim, unsigned G, float kWidth,
+                     const float *lut, int klength, double *mass, int threads);
+
 /* Tiles touched by each sample for a tile shape (tx,ty,tz): fills, per
  * sample, lo/hi tile coordinates (n*3 each).  Empty samples get lo > hi on
  * axis 0.  Used to check the device bin lists bit-for-bit. */

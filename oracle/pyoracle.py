@@ -48,6 +48,8 @@ class Oracle:
                                  C.c_float, _f32p, C.c_int, _f32p, C.c_int]
         lib.orc_grid_channel_f64.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_uint,
                                              C.c_float, _f32p, C.c_int, _f64p]
+        lib.orc_sample_mass.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _f32p, C.c_int, _f64p,
+                                        C.c_int]
         lib.orc_sample_tiles.argtypes = [_i32p, _i32p, C.c_size_t, C.c_int, _i32p, _i32p, _i32p]
         lib.orc_fft.argtypes = [_f32p, C.c_int, _u32p, C.c_int, C.c_int, C.c_int]
         lib.orc_fft_shift.argtypes = [_f32p, C.c_int, _u32p]
@@ -94,6 +96,13 @@ class Oracle:
         self.lib.orc_sample_tiles(np.ascontiguousarray(start, np.int32).ravel(),
                                   np.ascontiguousarray(end, np.int32).ravel(), n, dim, ts, lo, hi)
         return lo.reshape(n, 3), hi.reshape(n, 3)
+
+    def sample_mass(self, traj_norm4, dim, G, W, lut, threads=1) -> np.ndarray:
+        n = traj_norm4.shape[0]
+        out = np.zeros(n, np.float64)
+        self.lib.orc_sample_mass(np.ascontiguousarray(traj_norm4, np.float32), n, dim, G, W,
+                                 np.ascontiguousarray(lut, np.float32), len(lut), out, threads)
+        return out
 
     def grid(self, traj_norm4, dcf, kdata, dim, G, W, lut, threads=1) -> np.ndarray:
         """kdata: (C, N) complex64; returns (C, G^d) complex64."""

@@ -1,0 +1,84 @@
+"""CPU: the C-ABI library builds, loads, exports every symbol the header
+declares, and its host-only entry points behave (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from conftest import GOLDEN, ROOT
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "fastrecon_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char \*)\s*(fr_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    syms = header_symbols()
+    for s in ["fr_kb_lut", "fr_plan_create", "fr_plan_set_trajectory", "fr_grid", "fr_fft_create", "fr_sos",
+              "fr_recon_run", "fr_recon_run_host"]:
+        assert s in syms
+
+
+def test_library_exports_all_declared_symbols(frlib):
+    from fastrecon_gb300 import capi
+    for s in header_symbols():
+        assert hasattr(frlib, s), s
+    assert set(header_symbols()) <= set(capi.exported_symbols()) | set(header_symbols())
+    for s in capi.exported_symbols():
+        assert s in header_symbols(), f"binding {s} not declared in the header"
+
+
+def test_kb_lut_matches_reference_luts(frlib):
+    import fastrecon_gb300 as fr
+    z = np.load(os.path.join(GOLDEN, "luts.npz"))
+    for key in z.files:
+        w, o, l = key.split("_")
+        lut = fr.kb_lut(float(w[1:]), float(o[2:]), int(l[1:]))
+        assert np.array_equal(lut.view(np.uint32), z[key].view(np.uint32)), key
+
+
+def test_status_strings(frlib):
+    for s in range(10):
+        assert frlib.fr_status_string(s)
+    assert frlib.fr_status_string(0) == b"ok"
+    assert b"0.1" in frlib.fr_version()
+
+
+def test_argument_validation_without_gpu(frlib):
+    """Invalid descriptors are rejected before any CUDA call."""
+    from fastrecon_gb300 import capi
+    lut = (C.c_float * 512)()
+    d = capi.PlanDesc()
+    d.dim = 4
+    d.grid_size = 64
+    d.kernel_width = 4.0
+    d.lut_length = 512
+    d.lut = C.cast(lut, C.POINTER(C.c_float))
+    h = C.c_void_p()
+    assert frlib.fr_plan_create(C.byref(d), C.byref(h)) == 1  # FR_ERR_INVALID_ARGUMENT
+    assert b"dim" in frlib.fr_last_error()
+    d.dim = 2
+    d.grid_size = 0
+    assert frlib.fr_plan_create(C.byref(d), C.byref(h)) == 7  # FR_ERR_UNSUPPORTED
+    d.grid_size = 64
+    d.lut_length = 1
+    assert frlib.fr_plan_create(C.byref(d), C.byref(h)) == 1
+    assert frlib.fr_kb_lut(4.0, 2.0, 1, lut) == 1
+    assert frlib.fr_grid(None, None, None, 1, None, None) == 1
+    assert frlib.fr_fft_create(5, None, 1, 1, C.byref(h)) == 1
+    rd = capi.ReconDesc()
+    rd.dim = 2
+    rd.channels = 0
+    assert frlib.fr_recon_create(C.byref(rd), C.byref(h)) == 1
+
+
+def test_no_cpu_fallback_when_library_missing(tmp_path):
+    from fastrecon_gb300 import capi
+    try:
+        capi.load(str(tmp_path / "missing.so"))
+    except capi.FastreconError as e:
+        assert "not built" in str(e)
+    else:
+        raise AssertionError("loading a missing library must raise")
