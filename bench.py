@@ -39,6 +39,11 @@ WORKLOADS = {
                         dcf_power=2.0,
                         desc="3D radial kooshball: 50,000 golden-means spokes x 256 samples (12.8 M/coil), "
                              "16 coils, |k|^2 DCF, KB width 4, LUT 512, os 1.5 -> 384^3 grid, 256^3 SoS"),
+    # reduced kooshball with the same sample-density profile, for ncu captures
+    "kooshball3d_prof": dict(dim=3, spokes=12500, readout=128, coils=16, recon=128, os=1.5, width=4.0, lut=512,
+                             dcf_power=2.0,
+                             desc="reduced 3D kooshball for profiling: 12,500 golden-means spokes x 128 samples, "
+                                  "16 coils, os 1.5 -> 192^3 grid"),
     "radial2d": dict(dim=2, spokes=256, readout=512, coils=8, recon=256, os=2.0, width=4.0, lut=512,
                      dcf_power=1.0,
                      desc="2D radial: 256 spokes x 512 samples, 8 coils, |k| DCF, KB width 4, LUT 512, "
@@ -55,6 +60,8 @@ def parse():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="kooshball3d")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (ncu --profile-from-start off)")
     return ap.parse_args()
 
 
@@ -276,11 +283,15 @@ def run_ours(args, w):
     l0 = fr.kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if args.profile:
+        torch.cuda.profiler.start()
     e0.record(stream)
     for _ in range(args.steps):
         rec.run(traj, dcf, kd, out=img)
     e1.record(stream)
     barrier()
+    if args.profile:
+        torch.cuda.profiler.stop()
     ck = clocks.stop() if clocks else None
     launches = fr.kernel_launches() - l0
     elapsed = e0.elapsed_time(e1)  # ms

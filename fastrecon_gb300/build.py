@@ -80,7 +80,33 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_cpp_api(force=force)
     return LIB
+
+
+CPP_SRC = os.path.join(PKG, "cpp")
+CPP_LIB = os.path.join(LIBDIR, "libfastrecon.so")
+
+
+def build_cpp_api(force: bool = False) -> str:
+    """The C++ drop-in classes (ReconData, GridLut, ConvKernel, ImageFilter,
+    ImageData, cuImageData, ...) as libfastrecon.so on top of the C ABI."""
+    srcs = sorted(glob.glob(os.path.join(CPP_SRC, "*.cpp")))
+    hdrs = glob.glob(os.path.join(ROOT, "include", "fastrecon", "*.h")) + [os.path.join(ROOT, "include",
+                                                                                        "fastrecon_gb300.h")]
+    if not force and os.path.exists(CPP_LIB) and \
+            os.path.getmtime(CPP_LIB) >= max(os.path.getmtime(f) for f in srcs + hdrs + [LIB]):
+        return CPP_LIB
+    tmp = CPP_LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", os.path.join(ROOT, "include"), "-I",
+           os.path.join(CUDA_HOME, "include"), *srcs, "-o", tmp, "-L", LIBDIR, "-lfastrecon_gb300",
+           "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+           "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"C++ API build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CPP_LIB)
+    return CPP_LIB
 
 
 def clean():

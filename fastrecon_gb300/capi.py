@@ -64,6 +64,12 @@ _SIGS = {
     "fr_fft_shift": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), _VP]),
     "fr_crop": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), _VP, _VP]),
     "fr_sos": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), _VP, _VP, _VP]),
+    "fr_normalize_trajectory": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_uint, _VP, C.POINTER(C.c_float), _VP]),
+    "fr_transform_trajectory": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_float, C.c_float, _VP]),
+    "fr_real_to_complex": (C.c_int, [_VP, C.c_size_t, _VP, _VP]),
+    "fr_low_filter": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.c_int, _VP]),
+    "fr_normalize_channels": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), _VP]),
+    "fr_sos_map": (C.c_int, [_VP, _VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), _VP, _VP]),
     "fr_recon_create": (C.c_int, [C.POINTER(ReconDesc), C.POINTER(_VP)]),
     "fr_recon_destroy": (C.c_int, [_VP]),
     "fr_recon_run": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP]),

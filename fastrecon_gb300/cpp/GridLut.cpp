@@ -1,0 +1,150 @@
+// GridLut.cpp / cuGridLut.cpp / ConvKernel.cpp -- gridding classes of the C++
+// drop-in API.  Interface: ReconData/GridLut.h:9-42, cuGridLut.h:31-57,
+// ConvKernel.h:7-22.  All gridding runs through the C ABI (fr_plan_*, fr_grid).
+#include <cstdlib>
+#include <iostream>
+
+#include "fastrecon/ConvKernel.h"
+#include "fastrecon/cuGridLut.h"
+#include "fastrecon_gb300.h"
+
+namespace {
+void fr_ok(int st, const char *what)
+{
+    if (st != FR_OK)
+        throw std::runtime_error(std::string(what) + ": " + fr_status_string(st) + ": " + fr_last_error());
+}
+}  // namespace
+
+// ConvKernel.cpp:7-30 (fr_kb_lut computes the same float/double sequence).
+ConvKernel::ConvKernel(float kWidth, float overGridFactor, int length)
+    : m_kWidth(kWidth), m_ogFactor(overGridFactor), m_length(length)
+{
+    auto data = std::make_shared<std::vector<float>>(length > 0 ? length : 0);
+    if (length >= 2) fr_ok(fr_kb_lut(kWidth, overGridFactor, length, data->data()), "fr_kb_lut");
+    m_kernelData = data;
+}
+
+ConvKernel::~ConvKernel() {}
+
+const std::vector<float> *ConvKernel::getKernelData() const { return m_kernelData.get(); }
+
+float ConvKernel::getKernelWidth() const { return m_kWidth; }
+
+template <typename T>
+GridLut<T>::GridLut(ReconData<T> &reconData) : m_associatedData(reconData)
+{
+}
+
+template <typename T>
+GridLut<T>::~GridLut()
+{
+    delete m_kernel;
+}
+
+template <typename T>
+std::shared_ptr<GridLut<T>> GridLut<T>::Create(ReconData<T> &reconData)
+{
+    auto cu = dynamic_cast<cuReconData<T> *>(&reconData);
+    if (cu == nullptr) {
+        std::cerr << "Error: GridLut needs the ReconData returned by ReconData::Create." << std::endl;
+        exit(1);
+    }
+    return std::shared_ptr<GridLut<T>>(new cuGridLut<T>(*cu));
+}
+
+// GridLut.cpp:41-51
+template <typename T>
+void GridLut<T>::plan(unsigned reconSize, float overGridFactor, float kWidth, unsigned klength)
+{
+    m_dim = m_associatedData.rcDim();
+    m_gridSize = unsigned(reconSize * overGridFactor);
+    delete m_kernel;
+    m_kernel = new ConvKernel(kWidth, overGridFactor, klength);
+    m_associatedData.normalizeTraj(m_gridSize);
+}
+
+template class GridLut<float>;
+
+// ---------------------------------------------------------------------------
+// cuGridLut
+// ---------------------------------------------------------------------------
+
+template <typename T>
+cuGridLut<T>::cuGridLut(cuReconData<T> &reconData) : GridLut<T>(reconData), m_cuData(reconData)
+{
+}
+
+template <typename T>
+cuGridLut<T>::~cuGridLut()
+{
+    if (m_plan) fr_plan_destroy(m_plan);
+}
+
+template <typename T>
+void cuGridLut<T>::setTiling(int tx, int ty, int tz, int coilGroup)
+{
+    m_tile[0] = tx;
+    m_tile[1] = ty;
+    m_tile[2] = tz;
+    m_coil_group = coilGroup;
+}
+
+template <typename T>
+void cuGridLut<T>::plan(unsigned reconSize, float overGridFactor, float kWidth, unsigned klength)
+{
+    GridLut<T>::plan(reconSize, overGridFactor, kWidth, klength);  // normalises the trajectory in place
+    if (m_plan) {
+        fr_plan_destroy(m_plan);
+        m_plan = nullptr;
+    }
+    const std::vector<float> *lut = this->m_kernel->getKernelData();
+    fr_plan_desc d = {};
+    d.dim = (int)this->m_dim;
+    d.grid_size = this->m_gridSize;
+    d.kernel_width = kWidth;
+    d.lut_length = (int)lut->size();
+    d.lut = lut->data();
+    for (int i = 0; i < 3; ++i) d.tile[i] = m_tile[i];
+    int cg = m_coil_group;
+    if (cg <= 0) {
+        cg = 4;
+        while (cg < m_cuData.channels() && cg < 16) cg <<= 1;
+    }
+    d.coil_group = cg;
+    d.flags = FR_PLAN_PRENORMALIZED;
+    fr_ok(fr_plan_create(&d, &m_plan), "fr_plan_create");
+    const auto &traj = m_cuData.cuGetTraj();
+    fr_ok(fr_plan_set_trajectory(m_plan, reinterpret_cast<const float *>(traj.data()), traj.size(), nullptr),
+          "fr_plan_set_trajectory");
+}
+
+template <typename T>
+void cuGridLut<T>::executeInto(cuImageData<T> &img)
+{
+    fr_ok(fr_grid(m_plan, reinterpret_cast<const float *>(m_cuData.cuGetAllChannels()),
+                  reinterpret_cast<const float *>(m_cuData.cuGetDcf().data()), m_cuData.channels(),
+                  reinterpret_cast<float *>(img.cuData()), nullptr),
+          "fr_grid");
+    img.cuMarkModified();
+}
+
+// cuGridLut.cu:28-48: all channels in one launch instead of one per channel.
+template <typename T>
+std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
+{
+    if (m_plan == nullptr) {
+        std::cerr << "Error: run cuGridLut<T> first.";
+        exit(1);
+    }
+    const unsigned G = this->m_gridSize;
+    ImageSize size = {G, G, this->m_dim == 3 ? G : 1u};
+    auto img = std::make_shared<cuImageData<T>>((int)this->m_dim, size);
+    const int C = m_cuData.channels();
+    cuComplexVector<T> buf(img->dataSize() * (std::size_t)C);
+    img->cuReset((int)this->m_dim, size, C, std::move(buf));
+    executeInto(*img);
+    return img;
+}
+
+template class cuGridLut<float>;

@@ -128,8 +128,8 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
     *out = nullptr;
     if (d->dim != 2 && d->dim != 3) return fail(FR_ERR_INVALID_ARGUMENT, "dim must be 2 or 3");
     if (d->grid_size < 1 || d->grid_size > 4096) return fail(FR_ERR_UNSUPPORTED, "grid size must be in [1, 4096]");
-    if (!(d->kernel_width > 0.f) || d->kernel_width > 16.f)
-        return fail(FR_ERR_UNSUPPORTED, "kernel width must be in (0, 16]");
+    if (!(d->kernel_width > 0.f) || d->kernel_width > 13.f)
+        return fail(FR_ERR_UNSUPPORTED, "kernel width must be in (0, 13]");
     if (d->lut_length < 2 || d->lut_length > 16384 || !d->lut)
         return fail(FR_ERR_INVALID_ARGUMENT, "lut must have 2..16384 entries");
     auto p = new (std::nothrow) fr_plan_s;
@@ -155,14 +155,16 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
     }
     long long K = (long long)tile[0] * tile[1] * tile[2];
     int R = floats_per_cell(cg);
-    size_t smem = (size_t)K * R * 4 + (size_t)p->L * 4;
+    size_t smem = grid_smem_bytes(K, R, p->L);
     if (smem > 227 * 1024) {
         delete p;
         return fail(FR_ERR_UNSUPPORTED, "tile x coil group does not fit in shared memory");
     }
-    if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1 || tile[0] % (32 / std::min(R, 32)) != 0) {
+    if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1 || tile[0] > 64 || tile[1] > 64 || tile[2] > 64 ||
+        tile[0] % (32 / std::min(R, 32)) != 0) {
         delete p;
-        return fail(FR_ERR_UNSUPPORTED, "tile x extent must be a multiple of 32 / floats per cell");
+        return fail(FR_ERR_UNSUPPORTED,
+                    "tile extents must be 1..64 and x a multiple of 32 / floats per cell");
     }
     p->coil_group = cg;
     p->ntiles = 1;
@@ -177,6 +179,11 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         return fail(FR_ERR_UNSUPPORTED, "too many tiles");
     }
     p->chunk = d->chunk > 0 ? d->chunk : 4096;
+    {
+        // exact when hw^2 is representable and sqrt rounds back to hw
+        float h2 = p->hw * p->hw;
+        p->prefilter = (std::sqrt(h2) == p->hw) && ((double)h2 == (double)p->hw * (double)p->hw);
+    }
     if (p->lut_d.reserve((size_t)p->L * 4)) {
         delete p;
         return FR_ERR_OUT_OF_MEMORY;
@@ -249,8 +256,8 @@ int fr_plan_bins(fr_plan p, long long *d_tile_offset, unsigned *d_pairs, void *s
     // tile offsets are the .pairs field of the exclusive TileScan
     FR_CUDA(cudaMemcpy2DAsync(d_tile_offset, sizeof(long long), p->tile_scan.ptr, sizeof(TileScan),
                               sizeof(long long), (size_t)p->ntiles + 1, cudaMemcpyDeviceToDevice, s));
-    if (p->npairs)
-        FR_CUDA(cudaMemcpyAsync(d_pairs, p->pairs.ptr, (size_t)p->npairs * 4, cudaMemcpyDeviceToDevice, s));
+    if (p->npairs)  // the sample index is the low word of each 8-byte record
+        FR_CUDA(cudaMemcpy2DAsync(d_pairs, 4, p->pairs.ptr, 8, 4, (size_t)p->npairs, cudaMemcpyDeviceToDevice, s));
     return FR_OK;
 }
 
@@ -373,6 +380,61 @@ int fr_sos(const float *d_imgs, int channels, int dim, const unsigned *size, con
     if (!d_imgs || !d_out || !size || !recon || channels < 1 || (dim != 2 && dim != 3))
         return fail(FR_ERR_INVALID_ARGUMENT, "bad sos arguments");
     return sos_run(d_imgs, channels, dim, size, recon, d_deapod, d_out, (cudaStream_t)stream);
+}
+
+int fr_normalize_trajectory(const float *d_traj, size_t n, int dim, unsigned grid_size, float *d_out,
+                            float *bounds12, void *stream)
+{
+    if ((n && (!d_traj || !d_out)) || (dim != 2 && dim != 3) || grid_size < 1)
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad normalize arguments");
+    return normalize_run(d_traj, n, dim, grid_size, d_out, bounds12, (cudaStream_t)stream);
+}
+
+int fr_transform_trajectory(float *d_traj, size_t n, int dim, float translation, float scale, void *stream)
+{
+    if ((n && !d_traj) || dim < 1 || dim > 3) return fail(FR_ERR_INVALID_ARGUMENT, "bad transform arguments");
+    return transform_run(d_traj, n, dim, translation, scale, (cudaStream_t)stream);
+}
+
+int fr_real_to_complex(const float *d_in, size_t n, float *d_out, void *stream)
+{
+    if (n && (!d_in || !d_out)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return real_to_complex_run(d_in, n, d_out, (cudaStream_t)stream);
+}
+
+int fr_low_filter(float *d_imgs, int channels, int dim, const unsigned *size, int res, void *stream)
+{
+    if (!d_imgs || !size || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad low filter arguments");
+    // ImageFilter.cpp:62-68: att = 2 res^2 / 4 (double, stored float) and
+    // coeff[r] = expf(-r / 100.0) for r < 2000, evaluated on the host.
+    float att = (float)(2.0 * res * res / 4.0);
+    float coeff[2000];
+    for (int r = 0; r < 2000; r++) coeff[r] = expf((float)(-r / 100.0));
+    cudaStream_t s = (cudaStream_t)stream;
+    float *d_coeff = nullptr;
+    FR_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&d_coeff), sizeof(coeff), s));
+    FR_CUDA(cudaMemcpyAsync(d_coeff, coeff, sizeof(coeff), cudaMemcpyHostToDevice, s));
+    int st = low_filter_run(d_imgs, channels, dim, size, att, d_coeff, s);
+    cudaFreeAsync(d_coeff, s);
+    // the host table must outlive the async copy
+    FR_CUDA(cudaStreamSynchronize(s));
+    return st;
+}
+
+int fr_normalize_channels(float *d_imgs, int channels, int dim, const unsigned *size, void *stream)
+{
+    if (!d_imgs || !size || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad normalize arguments");
+    return normalize_channels_run(d_imgs, channels, dim, size, (cudaStream_t)stream);
+}
+
+int fr_sos_map(const float *d_imgs, const float *d_maps, int channels, int dim, const unsigned *size,
+               const unsigned *recon, float *d_out, void *stream)
+{
+    if (!d_imgs || !d_maps || !d_out || !size || !recon || channels < 1 || (dim != 2 && dim != 3))
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad sos arguments");
+    return sos_map_run(d_imgs, d_maps, channels, dim, size, recon, d_out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

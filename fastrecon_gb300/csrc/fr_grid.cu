@@ -28,7 +28,7 @@ namespace {
 
 struct GridParams {
     const float4 *traj;
-    const unsigned *pairs;
+    const unsigned long long *recs;  // sample index | tap box << 32, sorted by tile
     const WorkItem *items;
     const SplitTile *splits;
     const float *kdata;  // channels x n complex64, as floats
@@ -42,7 +42,7 @@ struct GridParams {
     int tile[3], ntile[3], K;
     int L;
     float hw, inv_hw, lm1;
-    int hw_pow2, prefilter, checkerboard;
+    int hw_pow2, checkerboard;
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -58,40 +58,77 @@ __device__ __forceinline__ int swz(int i)
     }
 }
 
+// Flush (or zero-fill) the tile's cells for one coil group.  Threads map to
+// (x, row) so consecutive lanes write consecutive x cells; row coordinates
+// advance incrementally (no divisions in the loop).
 template <int R>
 __device__ __forceinline__ void write_cell_group(const GridParams &P, const float *acc, int cg, int ox,
                                                  int oy, int oz, bool zero)
 {
     const int CG = P.coil_group;
-    const int K = P.K;
-    const int Tx = P.tile[0], Ty = P.tile[1];
+    const int Tx = P.tile[0], Ty = P.tile[1], Tz = P.tile[2];
+    const int ncl = min(CG, P.channels - cg * CG);
     const size_t G = (size_t)P.G;
+    const int Gz = P.dim == 3 ? P.G : 1;
     const size_t cells = P.dim == 3 ? G * G * G : G * G;
+    const int rows = Ty * Tz;
     float2 *grid = reinterpret_cast<float2 *>(P.grid);
-    const int total = CG * K;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    if ((int)blockDim.x % Tx == 0) {
+        const int lx = threadIdx.x % Tx, rr0 = threadIdx.x / Tx, rstep = blockDim.x / Tx;
+        const int dy = rstep % Ty, dz = rstep / Ty;
+        const int gx = ox + lx;
+        const bool xin = gx < P.G;
+        for (int cl = 0; cl < ncl; ++cl) {
+            const size_t cbase = (size_t)(cg * CG + cl) * cells;
+            int ly = rr0 % Ty, lz = rr0 / Ty;
+            for (int r = rr0; r < rows; r += rstep) {
+                const int gy = oy + ly, gz = oz + lz;
+                if (xin && gy < P.G && gz < Gz) {
+                    float2 v = make_float2(0.f, 0.f);
+                    if (!zero) {
+                        const int i = r * Tx + lx;
+                        v = *reinterpret_cast<const float2 *>(acc + (size_t)i * R + ((2 * cl) ^ swz<R>(i)));
+                        if (P.checkerboard && ((gx + gy + gz) & 1)) {
+                            v.x = -v.x;
+                            v.y = -v.y;
+                        }
+                    }
+                    grid[cbase + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+                }
+                ly += dy;
+                lz += dz;
+                if (ly >= Ty) {
+                    ly -= Ty;
+                    ++lz;
+                }
+            }
+        }
+        return;
+    }
+    const int K = P.K;
+    for (int idx = threadIdx.x; idx < ncl * K; idx += blockDim.x) {
         int cl = idx / K;
         int i = idx - cl * K;
-        int c = cg * CG + cl;
-        if (c >= P.channels) break;
         int lx = i % Tx;
         int r = i / Tx;
         int ly = r % Ty;
         int lz = r / Ty;
         int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        if (gx >= P.G || gy >= P.G || gz >= (P.dim == 3 ? P.G : 1)) continue;
+        if (gx >= P.G || gy >= P.G || gz >= Gz) continue;
         float2 v = make_float2(0.f, 0.f);
         if (!zero) {
-            int col = (2 * cl) ^ swz<R>(i);
-            v = *reinterpret_cast<const float2 *>(acc + (size_t)i * R + col);
+            v = *reinterpret_cast<const float2 *>(acc + (size_t)i * R + ((2 * cl) ^ swz<R>(i)));
             if (P.checkerboard && ((gx + gy + gz) & 1)) {
                 v.x = -v.x;
                 v.y = -v.y;
             }
         }
-        grid[(size_t)c * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+        grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
     }
 }
+
+constexpr int kWarps = 16;         // 512 threads per CTA
+constexpr int kListEntries = 32;   // per warp and buffer
 
 template <int DIM, int R>
 __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
@@ -100,6 +137,11 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
     float *acc = reinterpret_cast<float *>(smem4);
     const int K = P.K;
     float *lut = acc + (size_t)K * R;
+    // per warp, two buffers of a compacted tap list: {word offset of the
+    // tap's cell row (swizzled), weight}
+    int2 *lists = reinterpret_cast<int2 *>(lut + ((P.L + 3) & ~3));
+    // tap decode for boxes up to 4x4x4: dec[(nx-1)*4 + (ny-1)][t] = ix | iy<<2 | iz<<4
+    unsigned char *dec = reinterpret_cast<unsigned char *>(lists + kWarps * 2 * kListEntries);
 
     const WorkItem it = P.items[blockIdx.x];
     const int cg = blockIdx.y;
@@ -116,121 +158,117 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
 
     for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lut[i] = P.lut[i];
+    for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
+        const int nx = (i >> 8) + 1, ny = ((i >> 6) & 3) + 1, tt = i & 63;
+        const int ix = tt % nx, iy = (tt / nx) % ny, iz = tt / (nx * ny);
+        dec[i] = (unsigned char)(ix | (iy << 2) | ((iz & 3) << 4));
+    }
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int nwarps = blockDim.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     constexpr int NG = R >= 32 ? 1 : 32 / R;  // taps per accumulate step
     constexpr int NF = R > 32 ? R / 32 : 1;   // floats per lane per tap
     const int q = R >= 32 ? 0 : lane / R;     // tap slot of this lane
     const int f0 = R >= 32 ? lane : lane % R; // first coil float of this lane
     const int CG = P.coil_group;
-    const int hx = ox + P.tile[0] - 1, hy = oy + P.tile[1] - 1, hz = oz + P.tile[2] - 1;
+    const int Tx = P.tile[0], Ty = P.tile[1];
+    int2 *mylist = lists + warp * 2 * kListEntries;
+    int buf = 0;
 
-    int coil[NF];
+    const float *kdf[NF];
     bool coil_ok[NF];
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-        int f = f0 + 32 * k;
-        coil[k] = cg * CG + (f >> 1);
-        coil_ok[k] = (f >> 1) < CG && coil[k] < P.channels;
+        const int f = f0 + 32 * k;
+        const int coil = cg * CG + (f >> 1);
+        coil_ok[k] = (f >> 1) < CG && coil < P.channels;
+        // real or imaginary float of this coil's sample s is kdf[k][2 * s]
+        kdf[k] = P.kdata + 2 * (size_t)(coil_ok[k] ? coil : 0) * (size_t)P.n + (f & 1);
     }
-    const float2 *kd = reinterpret_cast<const float2 *>(P.kdata);
+    const unsigned long long *recs = P.recs + it.begin;
 
-    for (int j = warp; j < it.count; j += nwarps) {
-        const unsigned s = P.pairs[it.begin + j];
+    for (int j = warp; j < it.count; j += kWarps) {
+        const unsigned long long rec = recs[j];
+        const unsigned s = (unsigned)rec;
+        const unsigned box = (unsigned)(rec >> 32);
+        // tap box inside this tile, precomputed by the plan from the
+        // reference cell range (GridLut.cpp:98-106)
+        const int lx0 = box & 63, ly0 = (box >> 6) & 63, lz0 = (box >> 12) & 63;
+        const int nx = (box >> 18) & 15, ny = (box >> 22) & 15, nz = (box >> 26) & 15;
+        const int ntap = nx * ny * nz;
+        if (ntap == 0) continue;
         const float4 p = P.traj[s];
         const float d = P.dcf[s];
         float val[NF];
 #pragma unroll
-        for (int k = 0; k < NF; ++k) {
-            val[k] = 0.f;
-            if (coil_ok[k]) {
-                float2 z = kd[(size_t)coil[k] * (size_t)P.n + s];
-                // GridLut.cpp:109: data = dcf * sample
-                val[k] = __fmul_rn(d, ((f0 + 32 * k) & 1) ? z.y : z.x);
-            }
-        }
-        // Clamped cell range (GridLut.cpp:98-106), clipped to this tile.
-        int sx, ex, sy, ey, sz = 0, ez = 0;
-        comp_range(p.x, P.hw, (unsigned)P.G, sx, ex);
-        comp_range(p.y, P.hw, (unsigned)P.G, sy, ey);
-        if (DIM == 3) comp_range(p.z, P.hw, (unsigned)P.G, sz, ez);
-        sx = max(sx, ox); ex = min(ex, hx);
-        sy = max(sy, oy); ey = min(ey, hy);
-        if (DIM == 3) { sz = max(sz, oz); ez = min(ez, hz); }
-        if (P.prefilter) {
-            // Drop end taps with |d| >= kHW: with kHW^2 exact such taps
-            // have dk >= kHW, so the valid set is unchanged.
-            if (sx <= ex && !(fabsf(__fsub_rn((float)sx, p.x)) < P.hw)) ++sx;
-            if (sx <= ex && !(fabsf(__fsub_rn((float)ex, p.x)) < P.hw)) --ex;
-            if (sy <= ey && !(fabsf(__fsub_rn((float)sy, p.y)) < P.hw)) ++sy;
-            if (sy <= ey && !(fabsf(__fsub_rn((float)ey, p.y)) < P.hw)) --ey;
-            if (DIM == 3) {
-                if (sz <= ez && !(fabsf(__fsub_rn((float)sz, p.z)) < P.hw)) ++sz;
-                if (sz <= ez && !(fabsf(__fsub_rn((float)ez, p.z)) < P.hw)) --ez;
-            }
-        }
-        const int nx = ex - sx + 1, ny = ey - sy + 1, nz = ez - sz + 1;
-        if (nx <= 0 || ny <= 0 || nz <= 0) continue;
-        const int ntap = nx * ny * nz;
+        for (int k = 0; k < NF; ++k)
+            val[k] = coil_ok[k] ? __fmul_rn(d, kdf[k][2 * (size_t)s]) : 0.f;  // GridLut.cpp:109
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
-        // Small footprints use a fixed 4x4(x4) lane layout: one round in 2D,
-        // one or two (z pairs) in 3D.
-        const int nround = small ? (DIM == 3 && nz > 2 ? 2 : 1) : (ntap + 31) / 32;
+        const unsigned char *dtab = dec + (((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64;
+        const int nround = (ntap + 31) >> 5;
         for (int rnd = 0; rnd < nround; ++rnd) {
-            int ix, iy, iz;
-            bool ok;
-            if (small) {
-                int tt = rnd * 32 + lane;
-                ix = tt & 3;
-                iy = (tt >> 2) & 3;
-                iz = tt >> 4;
-                ok = ix < nx && iy < ny && iz < nz;
-            } else {
-                int tt = rnd * 32 + lane;
-                ok = tt < ntap;
-                ix = tt % nx;
-                int r = tt / nx;
-                iy = r % ny;
-                iz = r / ny;
-            }
-            int cell = 0;
-            float w = 0.f;
+            const int tt = rnd * 32 + lane;
+            bool ok = tt < ntap;
+            int ix = 0, iy = 0, iz = 0;
             if (ok) {
-                int x = sx + ix, y = sy + iy, z = sz + iz;
-                float dx = __fsub_rn((float)x, p.x);
-                float dy = __fsub_rn((float)y, p.y);
-                float dz = DIM == 3 ? __fsub_rn((float)z, p.z) : 0.f;
-                int ki = tap_index(dx, __fmul_rn(dy, dy), __fmul_rn(dz, dz), P.hw, P.inv_hw, P.hw_pow2,
-                                   P.lm1, P.L);
+                if (small) {
+                    const int code = dtab[tt];
+                    ix = code & 3;
+                    iy = (code >> 2) & 3;
+                    iz = code >> 4;
+                } else {
+                    ix = tt % nx;
+                    const int r = tt / nx;
+                    iy = r % ny;
+                    iz = r / ny;
+                }
+            }
+            int2 e = make_int2(0, 0);
+            if (ok) {
+                const int lx = lx0 + ix, ly = ly0 + iy, lz = lz0 + iz;
+                const float dx = __fsub_rn((float)(ox + lx), p.x);
+                const float dy = __fsub_rn((float)(oy + ly), p.y);
+                const float dz = DIM == 3 ? __fsub_rn((float)(oz + lz), p.z) : 0.f;
+                const int ki = tap_index(dx, __fmul_rn(dy, dy), __fmul_rn(dz, dz), P.hw, P.inv_hw, P.hw_pow2,
+                                         P.lm1, P.L);
                 ok = ki >= 0;
                 if (ok) {
-                    w = lut[ki];
-                    cell = ((z - oz) * P.tile[1] + (y - oy)) * P.tile[0] + (x - ox);
+                    const int cell = (lz * Ty + ly) * Tx + lx;
+                    e = make_int2(cell * R + swz<R>(cell), __float_as_int(lut[ki]));
                 }
             }
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            while (m) {
-                int src[NG];
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (m == 0) continue;
+            int2 *lst = mylist + buf * kListEntries;
+            buf ^= 1;
+            if (ok) lst[__popc(m & lt)] = e;
+            __syncwarp();
+            const int n = __popc(m);
+            if (NG == 1) {
+                int k = 0;
+                for (; k + 1 < n; k += 2) {
+                    const int4 e2 = *reinterpret_cast<const int4 *>(lst + k);
 #pragma unroll
-                for (int g = 0; g < NG; ++g) {
-                    src[g] = m ? __ffs(m) - 1 : -1;
-                    m &= m - 1;
+                    for (int kk = 0; kk < NF; ++kk) {
+                        if (coil_ok[kk]) {
+                            atomicAdd(acc + ((e2.x ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e2.y), val[kk]));
+                            atomicAdd(acc + ((e2.z ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e2.w), val[kk]));
+                        }
+                    }
                 }
-                int mysrc = src[0];
+                if (k < n) {
+                    const int2 e1 = lst[k];
 #pragma unroll
-                for (int g = 1; g < NG; ++g)
-                    if (q == g) mysrc = src[g];
-                int cq = __shfl_sync(0xffffffffu, cell, mysrc & 31);
-                float wq = __shfl_sync(0xffffffffu, w, mysrc & 31);
-                if (mysrc >= 0) {
-                    float *row = acc + (size_t)cq * R;
-                    const int sw = swz<R>(cq);
-#pragma unroll
-                    for (int k = 0; k < NF; ++k)
-                        if (coil_ok[k]) atomicAdd(row + ((f0 + 32 * k) ^ sw), __fmul_rn(wq, val[k]));
+                    for (int kk = 0; kk < NF; ++kk)
+                        if (coil_ok[kk])
+                            atomicAdd(acc + ((e1.x ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e1.y), val[kk]));
+                }
+            } else {
+                for (int k = q; k < n; k += NG) {
+                    const int2 e1 = lst[k];
+                    if (coil_ok[0]) atomicAdd(acc + (e1.x ^ f0), __fmul_rn(__int_as_float(e1.y), val[0]));
                 }
             }
         }
@@ -292,7 +330,7 @@ __global__ void reduce_splits_kernel(GridParams P)
 template <int DIM, int R>
 int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, cudaStream_t s)
 {
-    size_t smem = (size_t)P.K * R * 4 + (size_t)P.L * 4;
+    size_t smem = grid_smem_bytes(P.K, R, P.L);
     static_assert(R % 4 == 0, "rows of whole float4");
     auto kern = grid_tiles_kernel<DIM, R>;
     if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -324,6 +362,12 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
 
 }  // namespace
 
+size_t grid_smem_bytes(long long K, int R, int L)
+{
+    // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode table
+    return (size_t)K * R * 4 + (size_t)((L + 3) & ~3) * 4 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64;
+}
+
 int floats_per_cell(int coil_group)
 {
     int r = 8;
@@ -353,7 +397,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     const int R = floats_per_cell(p->coil_group);
     GridParams P;
     P.traj = p->traj.as<float4>();
-    P.pairs = p->pairs.as<unsigned>();
+    P.recs = p->pairs.as<unsigned long long>();
     P.items = p->items.as<WorkItem>();
     P.splits = p->splits.as<SplitTile>();
     P.kdata = d_kdata;
@@ -379,11 +423,6 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.hw_pow2 = (m == 0.5f);
     P.inv_hw = P.hw_pow2 ? ldexpf(1.0f, 1 - e) : 0.f;
     P.lm1 = (float)(p->L - 1);
-    {
-        // Prefilter is exact when sqrt(fl(hw*hw)) rounds back to hw.
-        float h2 = p->hw * p->hw;
-        P.prefilter = (sqrtf(h2) == p->hw) && (h2 == (double)p->hw * (double)p->hw);
-    }
     P.checkerboard = (p->flags & FR_PLAN_CHECKERBOARD) ? 1 : 0;
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;

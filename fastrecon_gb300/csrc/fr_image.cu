@@ -283,3 +283,134 @@ int deapod_map_run(const float *d_img, int dim, const unsigned *size, const unsi
 }
 
 }  // namespace fr
+
+// --------------------------------------------------------------------------
+// PILS image operations (ImageFilter.cpp:55-118,170-209) and helpers.
+// --------------------------------------------------------------------------
+namespace fr {
+namespace {
+
+__global__ void real_to_complex_kernel(const float *__restrict__ in, size_t n, float2 *__restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = make_float2(in[i], 0.f);
+}
+
+// ImageFilter::lowFilter: r = squared distance to (size/2) in integers,
+// idx = (int)((float)r / att * 100.0), coefficient table from the host.
+__global__ void low_filter_kernel(float2 *__restrict__ imgs, int channels, Size3 s, float att,
+                                  const float *__restrict__ coeff)
+{
+    const size_t cells = (size_t)s.x * s.y * s.z;
+    const size_t total = cells * (size_t)channels;
+    const long long x0 = s.x / 2, y0 = s.y / 2, z0 = s.z / 2;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < total; o += (size_t)gridDim.x * blockDim.x) {
+        size_t v = o % cells;
+        long long x = (long long)(v % s.x);
+        size_t r0 = v / s.x;
+        long long y = (long long)(r0 % s.y);
+        long long z = (long long)(r0 / s.y);
+        int r = (int)((x - x0) * (x - x0) + (y - y0) * (y - y0) + (z - z0) * (z - z0));
+        int idx = (int)((double)__fdiv_rn((float)r, att) * 100.0);
+        float2 a = imgs[o];
+        if (idx >= 2000) {
+            a = make_float2(0.f, 0.f);
+        } else {
+            float c = coeff[idx];
+            a.x = __fmul_rn(a.x, c);
+            a.y = __fmul_rn(a.y, c);
+        }
+        imgs[o] = a;
+    }
+}
+
+// ImageFilter::normalize: mag = sum over channels of std::norm, each value
+// divided by sqrtf(mag).
+__global__ void normalize_channels_kernel(float2 *__restrict__ imgs, int channels, size_t cells)
+{
+    for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < cells; v += (size_t)gridDim.x * blockDim.x) {
+        float mag = 0.f;
+        for (int c = 0; c < channels; ++c) {
+            float2 a = imgs[(size_t)c * cells + v];
+            mag = __fadd_rn(mag, __fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y)));
+        }
+        float d = __fsqrt_rn(mag);
+        for (int c = 0; c < channels; ++c) {
+            float2 a = imgs[(size_t)c * cells + v];
+            imgs[(size_t)c * cells + v] = make_float2(__fdiv_rn(a.x, d), __fdiv_rn(a.y, d));
+        }
+    }
+}
+
+// ImageFilter::SOS(map, reconSize): out += data * conj(map) per channel.
+__global__ void sos_map_kernel(const float2 *__restrict__ imgs, const float2 *__restrict__ maps, int channels,
+                               Size3 in, Size3 rec, Size3 off, float2 *__restrict__ out)
+{
+    const size_t nout = (size_t)rec.x * rec.y * rec.z;
+    const size_t cells = (size_t)in.x * in.y * in.z;
+    for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < nout; o += (size_t)gridDim.x * blockDim.x) {
+        unsigned x = (unsigned)(o % rec.x);
+        size_t r = o / rec.x;
+        unsigned y = (unsigned)(r % rec.y);
+        unsigned z = (unsigned)(r / rec.y);
+        size_t in_idx = ((size_t)(z + off.z) * in.y + (y + off.y)) * in.x + (x + off.x);
+        float2 acc = make_float2(0.f, 0.f);
+        for (int c = 0; c < channels; ++c) {
+            float2 a = imgs[(size_t)c * cells + in_idx];
+            float2 m = maps[(size_t)c * cells + in_idx];
+            float nd = -m.y;  // conj
+            float re = __fsub_rn(__fmul_rn(a.x, m.x), __fmul_rn(a.y, nd));
+            float im = __fadd_rn(__fmul_rn(a.x, nd), __fmul_rn(a.y, m.x));
+            acc.x = __fadd_rn(acc.x, re);
+            acc.y = __fadd_rn(acc.y, im);
+        }
+        out[o] = acc;
+    }
+}
+
+}  // namespace
+
+int real_to_complex_run(const float *d_in, size_t n, float *d_out, cudaStream_t s)
+{
+    if (n == 0) return FR_OK;
+    real_to_complex_kernel<<<blocks_for(n, 256), 256, 0, s>>>(d_in, n, reinterpret_cast<float2 *>(d_out));
+    FR_CHECK_LAUNCH("real_to_complex_kernel");
+    return FR_OK;
+}
+
+int low_filter_run(float *d_imgs, int channels, int dim, const unsigned *size, float att, const float *d_coeff,
+                   cudaStream_t s)
+{
+    Size3 sz = size_of(dim, size);
+    size_t total = (size_t)sz.x * sz.y * sz.z * channels;
+    low_filter_kernel<<<blocks_for(total, 256), 256, 0, s>>>(reinterpret_cast<float2 *>(d_imgs), channels, sz, att,
+                                                            d_coeff);
+    FR_CHECK_LAUNCH("low_filter_kernel");
+    return FR_OK;
+}
+
+int normalize_channels_run(float *d_imgs, int channels, int dim, const unsigned *size, cudaStream_t s)
+{
+    Size3 sz = size_of(dim, size);
+    size_t cells = (size_t)sz.x * sz.y * sz.z;
+    normalize_channels_kernel<<<blocks_for(cells, 256), 256, 0, s>>>(reinterpret_cast<float2 *>(d_imgs), channels,
+                                                                    cells);
+    FR_CHECK_LAUNCH("normalize_channels_kernel");
+    return FR_OK;
+}
+
+int sos_map_run(const float *d_imgs, const float *d_maps, int channels, int dim, const unsigned *size,
+                const unsigned *recon, float *d_out, cudaStream_t s)
+{
+    Size3 in, r, off;
+    int st = check_crop(dim, size, recon, in, r, off);
+    if (st) return st;
+    size_t nout = (size_t)r.x * r.y * r.z;
+    sos_map_kernel<<<blocks_for(nout, 256), 256, 0, s>>>(reinterpret_cast<const float2 *>(d_imgs),
+                                                        reinterpret_cast<const float2 *>(d_maps), channels, in, r,
+                                                        off, reinterpret_cast<float2 *>(d_out));
+    FR_CHECK_LAUNCH("sos_map_kernel");
+    return FR_OK;
+}
+
+}  // namespace fr

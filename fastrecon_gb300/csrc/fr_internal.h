@@ -76,6 +76,7 @@ struct fr_plan_s {
     long long ntiles = 0;
     int coil_group = 8;
     int chunk = 4096;
+    int prefilter = 0;  // |x - c| >= kHW implies dk >= kHW (kHW^2 and sqrt exact)
     unsigned flags = 0;
 
     size_t n = 0;
@@ -90,7 +91,7 @@ struct fr_plan_s {
     fr::DevBuf tile_fill;     // ntiles int
     fr::DevBuf tile_scan;     // (ntiles + 1) TileScan, exclusive
     fr::DevBuf scan_blocks;   // scan scratch
-    fr::DevBuf pairs;         // npairs uint32
+    fr::DevBuf pairs;         // npairs records: sample index | tap box << 32
     fr::DevBuf items;         // nitems WorkItem
     fr::DevBuf splits;        // nsplits SplitTile
     fr::DevBuf partials;      // nslots * ngroups * K * R floats
@@ -118,6 +119,9 @@ int crop_run(const float *d_imgs, int channels, int dim, const unsigned *size, c
 void default_tiling(int dim, int *tile, int *coil_group, int channels);
 // Floats per tile cell in shared memory for a coil group.
 int floats_per_cell(int coil_group);
+// Dynamic shared memory of the scatter kernel for K cells of R floats and an
+// L-entry LUT.
+size_t grid_smem_bytes(long long K, int R, int L);
 }  // namespace fr
 
 namespace fr {
@@ -125,4 +129,16 @@ int deapod_seed_run(float *d_grid, int dim, int G, float hw, const float *d_lut,
                     cudaStream_t s);
 int deapod_map_run(const float *d_img, int dim, const unsigned *size, const unsigned *recon, float *d_out,
                    cudaStream_t s);
+}  // namespace fr
+
+namespace fr {
+int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_out, float *bounds12,
+                  cudaStream_t s);
+int transform_run(float *d_traj, size_t n, int dim, float tr, float scale, cudaStream_t s);
+int real_to_complex_run(const float *d_in, size_t n, float *d_out, cudaStream_t s);
+int low_filter_run(float *d_imgs, int channels, int dim, const unsigned *size, float att, const float *d_coeff,
+                   cudaStream_t s);
+int normalize_channels_run(float *d_imgs, int channels, int dim, const unsigned *size, cudaStream_t s);
+int sos_map_run(const float *d_imgs, const float *d_maps, int channels, int dim, const unsigned *size,
+                const unsigned *recon, float *d_out, cudaStream_t s);
 }  // namespace fr

@@ -108,6 +108,7 @@ struct BinGeom {
     int dim;
     unsigned G;
     float hw;
+    int prefilter;
     int tile[3];
     int ntile[3];
 };
@@ -148,8 +149,33 @@ __device__ __forceinline__ int tile_of(const BinGeom &g, const int *lo, const in
 // tile.  Counts are aggregated per warp over lanes that hit the same tile
 // (consecutive samples of a readout usually do), so a dense tile sees one
 // atomic per warp instead of one per sample.
+__device__ __forceinline__ float4 normalize_point(float4 p, int dim, float tr, float scale, int prenorm)
+{
+    float4 q;
+    if (prenorm) {
+        q.x = p.x;
+        q.y = dim > 1 ? p.y : 0.f;
+        q.z = dim > 2 ? p.z : 0.f;
+    } else {
+        q.x = __fmul_rn(__fadd_rn(p.x, tr), scale);
+        q.y = dim > 1 ? __fmul_rn(__fadd_rn(p.y, tr), scale) : 0.f;
+        q.z = dim > 2 ? __fmul_rn(__fadd_rn(p.z, tr), scale) : 0.f;
+    }
+    q.w = 0.f;
+    return q;
+}
+
+__global__ void normalize_kernel(const float4 *__restrict__ raw, size_t n, int dim, const int *__restrict__ b,
+                                 float4 *__restrict__ out)
+{
+    const float *bf = reinterpret_cast<const float *>(b);
+    const float tr = bf[kTr], scale = bf[kScale];
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = normalize_point(raw[i], dim, tr, scale, 0);
+}
+
 __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n, BinGeom g,
-                                       const int *__restrict__ b, float4 *__restrict__ out,
+                                       const int *__restrict__ b, int prenorm, float4 *__restrict__ out,
                                        int *__restrict__ tile_count)
 {
     const float *bf = reinterpret_cast<const float *>(b);
@@ -161,12 +187,7 @@ __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n,
         int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
         int cnt = 0;
         if (i < n) {
-            float4 p = raw[i];
-            float4 q;
-            q.x = __fmul_rn(__fadd_rn(p.x, tr), scale);
-            q.y = g.dim > 1 ? __fmul_rn(__fadd_rn(p.y, tr), scale) : 0.f;
-            q.z = g.dim > 2 ? __fmul_rn(__fadd_rn(p.z, tr), scale) : 0.f;
-            q.w = 0.f;
+            float4 q = normalize_point(raw[i], g.dim, tr, scale, prenorm);
             out[i] = q;
             cnt = sample_tiles(g, q, lo, hi);
         }
@@ -181,10 +202,38 @@ __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n,
     }
 }
 
-// Pass 3: fill the sorted bin lists.
+// Tap box of a sample inside one tile: the sample's clamped cell range
+// (GridLut.cpp:98-106) with end taps |x - c| >= kHW removed when that test
+// is exact (they can never pass dk < kHW), clipped to the tile, in tile-local
+// coordinates.  Packed as lx0 | ly0<<6 | lz0<<12 | nx<<18 | ny<<22 | nz<<26.
+__device__ __forceinline__ unsigned tile_box(const BinGeom &g, const float *c, const int *s, const int *e,
+                                             int tx, int ty, int tz)
+{
+    const int t3[3] = {tx, ty, tz};
+    unsigned box = 0;
+    for (int d = 0; d < 3; ++d) {
+        int lo = 0, num = 1;
+        if (d < g.dim) {
+            int o = t3[d] * g.tile[d];
+            int a = max(s[d], o), b = min(e[d], o + g.tile[d] - 1);
+            if (g.prefilter && a <= b) {
+                if (!(fabsf(__fsub_rn((float)a, c[d])) < g.hw)) ++a;
+                if (a <= b && !(fabsf(__fsub_rn((float)b, c[d])) < g.hw)) --b;
+            }
+            lo = a - o;
+            num = a <= b ? b - a + 1 : 0;
+            if (num == 0) lo = 0;
+        }
+        box |= (unsigned)lo << (6 * d);
+        box |= (unsigned)num << (18 + 4 * d);
+    }
+    return box;
+}
+
+// Pass 3: fill the sorted bin lists with (sample index, tap box) records.
 __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g,
                             const TileScan *__restrict__ scan, int *__restrict__ tile_fill,
-                            unsigned *__restrict__ pairs)
+                            unsigned long long *__restrict__ recs)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -192,10 +241,16 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
          base += (size_t)gridDim.x * blockDim.x) {
         size_t i = base + threadIdx.x;
         int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
+        int s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+        float c[3] = {0.f, 0.f, 0.f};
         int cnt = 0;
         if (i < n) {
             float4 q = traj[i];
             cnt = sample_tiles(g, q, lo, hi);
+            c[0] = q.x;
+            c[1] = q.y;
+            c[2] = q.z;
+            for (int d = 0; d < g.dim; ++d) comp_range(c[d], g.hw, g.G, s[d], e[d]);
         }
         int maxcnt = __reduce_max_sync(0xffffffffu, cnt);
         for (int j = 0; j < maxcnt; ++j) {
@@ -208,7 +263,11 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
             basepos = __shfl_sync(0xffffffffu, basepos, leader);
             if (valid) {
                 long long pos = scan[t].pairs + basepos + __popc(m & lt);
-                pairs[pos] = (unsigned)i;
+                int tx = t % g.ntile[0];
+                int ty = (t / g.ntile[0]) % g.ntile[1];
+                int tz = t / (g.ntile[0] * g.ntile[1]);
+                unsigned box = tile_box(g, c, s, e, tx, ty, tz);
+                recs[pos] = ((unsigned long long)box << 32) | (unsigned long long)i;
             }
         }
     }
@@ -413,14 +472,15 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     g.dim = p->dim;
     g.G = p->G;
     g.hw = p->hw;
+    g.prefilter = p->prefilter;
     for (int d = 0; d < 3; ++d) {
         g.tile[d] = p->tile[d];
         g.ntile[d] = p->ntile[d];
     }
     float4 *traj = p->traj.as<float4>();
     if (n > 0) {
-        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, traj,
-                                                                   p->tile_count.as<int>());
+        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(
+            raw, n, g, b, (p->flags & FR_PLAN_PRENORMALIZED) ? 1 : 0, traj, p->tile_count.as<int>());
         FR_CHECK_LAUNCH("normalize_count_kernel");
     }
     TileScan *bs = p->scan_blocks.as<TileScan>();
@@ -443,8 +503,9 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     // bounds_host: raw lo[3], raw hi[3], norm lo[3], norm hi[3]
     float norm_b[6];
     for (int i = 0; i < 6; ++i) norm_b[i] = p->bounds_host[i];
+    const bool prenorm = (p->flags & FR_PLAN_PRENORMALIZED) != 0;
     for (int i = 0; i < 6; ++i) p->bounds_host[i] = raw_b[i];
-    for (int i = 0; i < 6; ++i) p->bounds_host[6 + i] = norm_b[i];
+    for (int i = 0; i < 6; ++i) p->bounds_host[6 + i] = prenorm ? raw_b[i] : norm_b[i];
 
     if (tot.pairs > 0xFFFFFFFFll || tot.items > INT_MAX || tot.slots > INT_MAX)
         return fail(FR_ERR_UNSUPPORTED, "bin lists exceed 32-bit indexing");
@@ -452,13 +513,13 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     p->nitems = tot.items;
     p->nslots = tot.slots;
     p->nsplits = tot.splits;
-    if (p->pairs.reserve(std::max<long long>(tot.pairs, 1) * 4) ||
+    if (p->pairs.reserve(std::max<long long>(tot.pairs, 1) * 8) ||
         p->items.reserve(std::max<long long>(tot.items, 1) * sizeof(WorkItem)) ||
         p->splits.reserve(std::max<long long>(tot.splits, 1) * sizeof(SplitTile)))
         return FR_ERR_OUT_OF_MEMORY;
     if (n > 0) {
         fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, scan, p->tile_fill.as<int>(),
-                                                        p->pairs.as<unsigned>());
+                                                        p->pairs.as<unsigned long long>());
         FR_CHECK_LAUNCH("fill_kernel");
     }
     items_kernel<<<grid_blocks(p->ntiles, 256), 256, 0, s>>>(p->tile_count.as<int>(), scan, p->ntiles,
@@ -466,6 +527,59 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
                                                              p->splits.as<SplitTile>());
     FR_CHECK_LAUNCH("items_kernel");
     p->planned = true;
+    return FR_OK;
+}
+
+namespace {
+__global__ void transform_kernel(float4 *__restrict__ traj, size_t n, int dim, float tr, float scale)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float4 p = traj[i];
+        p.x = __fmul_rn(__fadd_rn(p.x, tr), scale);
+        if (dim > 1) p.y = __fmul_rn(__fadd_rn(p.y, tr), scale);
+        if (dim > 2) p.z = __fmul_rn(__fadd_rn(p.z, tr), scale);
+        traj[i] = p;
+    }
+}
+}  // namespace
+
+int transform_run(float *d_traj, size_t n, int dim, float tr, float scale, cudaStream_t s)
+{
+    if (reinterpret_cast<uintptr_t>(d_traj) & 15)
+        return fail(FR_ERR_INVALID_ARGUMENT, "trajectory pointer must be 16-byte aligned");
+    if (n == 0) return FR_OK;
+    transform_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(reinterpret_cast<float4 *>(d_traj), n, dim, tr, scale);
+    FR_CHECK_LAUNCH("transform_kernel");
+    return FR_OK;
+}
+
+int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_out, float *bounds12,
+                  cudaStream_t s)
+{
+    if ((reinterpret_cast<uintptr_t>(d_traj) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 15))
+        return fail(FR_ERR_INVALID_ARGUMENT, "trajectory pointers must be 16-byte aligned");
+    int *b = nullptr;
+    FR_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&b), kBoundsSlots * 4, s));
+    bounds_init_kernel<<<1, 32, 0, s>>>(b);
+    FR_CHECK_LAUNCH("bounds_init_kernel");
+    const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
+    if (n > 0) {
+        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, dim, b);
+        FR_CHECK_LAUNCH("bounds_kernel");
+    }
+    scale_kernel<<<1, 1, 0, s>>>(b, dim, G);
+    FR_CHECK_LAUNCH("scale_kernel");
+    if (n > 0) {
+        normalize_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, dim, b, reinterpret_cast<float4 *>(d_out));
+        FR_CHECK_LAUNCH("normalize_kernel");
+    }
+    float hb[12];
+    FR_CUDA(cudaMemcpyAsync(hb, reinterpret_cast<float *>(b) + kRawLo, 6 * 4, cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaMemcpyAsync(hb + 6, reinterpret_cast<float *>(b) + kNormLo, 6 * 4, cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaFreeAsync(b, s));
+    FR_CUDA(cudaStreamSynchronize(s));
+    if (bounds12)
+        for (int i = 0; i < 12; ++i) bounds12[i] = hb[i];
     return FR_OK;
 }
 

@@ -207,6 +207,33 @@ def sos(imgs, dim: int, G: int, recon, deapod=None, stream=None):
     return out
 
 
+def low_filter(imgs, dim: int, G: int, res: int, stream=None):
+    """ImageFilter::lowFilter(res) on (C, G^d) complex64, in place."""
+    lib = capi.load()
+    check(lib.fr_low_filter(_ptr(imgs), imgs.shape[0], dim, u3(_size3(dim, G)), res, C.c_void_p(_stream(stream))),
+          "fr_low_filter")
+    return imgs
+
+
+def normalize_channels(imgs, dim: int, G: int, stream=None):
+    """ImageFilter::normalize on (C, G^d) complex64, in place."""
+    lib = capi.load()
+    check(lib.fr_normalize_channels(_ptr(imgs), imgs.shape[0], dim, u3(_size3(dim, G)),
+                                    C.c_void_p(_stream(stream))), "fr_normalize_channels")
+    return imgs
+
+
+def sos_map(imgs, maps, dim: int, G: int, recon, stream=None):
+    """ImageFilter::SOS(map, reconSize): complex recon-size image."""
+    torch = _torch()
+    rs = list(recon) + [1] * (3 - len(recon))
+    out = torch.empty(int(np.prod(rs)), dtype=torch.complex64, device="cuda")
+    lib = capi.load()
+    check(lib.fr_sos_map(_ptr(imgs), _ptr(maps), imgs.shape[0], dim, u3(_size3(dim, G)), u3(rs), _ptr(out),
+                         C.c_void_p(_stream(stream))), "fr_sos_map")
+    return out
+
+
 class Recon:
     """The Program/Main.cpp pipeline as one object (fr_recon_*)."""
 

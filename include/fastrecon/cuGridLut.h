@@ -1,0 +1,40 @@
+// cuGridLut.h -- GPU gridding (ReconData/cuGridLut.h:31-57), backed by the
+// C ABI of libfastrecon_gb300.so (fr_plan_*, fr_grid).
+//
+// Differences from the reference: the plan belongs to this object and is
+// built for this object's trajectory (the reference caches one plan per
+// process, keyed on nothing, cuGridLut.cu:14-18,158-159); there are no host-side
+// partitions, so setNumOfPartitions only records the value.
+#ifndef FASTRECON_CUGRIDLUT_H
+#define FASTRECON_CUGRIDLUT_H
+
+#include "GridLut.h"
+#include "cuImageData.h"
+#include "cuReconData.h"
+
+struct fr_plan_s;
+
+template <typename T>
+class cuGridLut : public GridLut<T> {
+public:
+    cuGridLut(cuReconData<T> &reconData);
+    virtual ~cuGridLut();
+
+    virtual void plan(unsigned reconSize, float overGridFactor, float kWidth, unsigned klength = 32) override;
+    virtual std::shared_ptr<ImageData<T>> execute() override;
+    void setNumOfPartitions(int partitions) { m_gpu_partitions = partitions; }
+
+    // Tile shape and coils per scatter pass used by the next plan() (0 = default).
+    void setTiling(int tx, int ty, int tz, int coilGroup);
+    // Grid into an existing image whose device buffer holds channels x G^d (no allocation).
+    void executeInto(cuImageData<T> &img);
+
+private:
+    cuReconData<T> &m_cuData;
+    fr_plan_s *m_plan = nullptr;
+    int m_gpu_partitions = 1;
+    int m_tile[3] = {0, 0, 0};
+    int m_coil_group = 0;
+};
+
+#endif  // FASTRECON_CUGRIDLUT_H

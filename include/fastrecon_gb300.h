@@ -68,10 +68,29 @@ int fr_kb_lut(float kernel_width, float overgrid_factor, int length, float *lut_
 typedef struct fr_plan_s *fr_plan;
 
 enum {
-    FR_PLAN_CHECKERBOARD = 1u << 0 /* multiply grid cell (x,y,z) by (-1)^(x+y+z)
-                                      on output, which makes the backward FFT
-                                      produce the fftShift-ed image (even G) */
+    FR_PLAN_CHECKERBOARD = 1u << 0, /* multiply grid cell (x,y,z) by (-1)^(x+y+z)
+                                       on output, which makes the backward FFT
+                                       produce the fftShift-ed image (even G) */
+    FR_PLAN_PRENORMALIZED = 1u << 1 /* the trajectory given to
+                                       fr_plan_set_trajectory is already in
+                                       grid units (ReconData::normalizeTraj was
+                                       applied, e.g. by fr_normalize_trajectory):
+                                       bin it as is */
 };
+
+/* ReconData::normalizeTraj (ReconData.cpp:211-225) on the device: component
+ * bounds of d_traj (n Point<float>), translation -min and scale
+ * (G-1)/(max-min) of component 0, x <- (x + tr) * scale for components < dim
+ * into d_out (may equal d_traj).  bounds12 (host, nullable) receives raw
+ * lo[3], raw hi[3], normalised lo[3], normalised hi[3].  Synchronises
+ * `stream`. */
+int fr_normalize_trajectory(const float *d_traj, size_t n, int dim, unsigned grid_size, float *d_out,
+                            float *bounds12, void *stream);
+
+/* cuReconData::transformLocalTraj (cuReconData.cu:88-99, scale_functor
+ * cuReconData.h:23-37): x <- (x + translation) * scale for components < dim
+ * of n Point<float> samples, in place on the device. */
+int fr_transform_trajectory(float *d_traj, size_t n, int dim, float translation, float scale, void *stream);
 
 typedef struct {
     int dim;               /* 2 or 3 (ReconData::rcDim) */
@@ -161,6 +180,22 @@ int fr_crop(const float *d_imgs, int channels, int dim, const unsigned *size,
  * the reference; NULL reproduces the reference). */
 int fr_sos(const float *d_imgs, int channels, int dim, const unsigned *size,
            const unsigned *recon, const float *d_deapod, float *d_out, void *stream);
+
+/* (m, 0) complex from n real values, device to device: the complex image the
+ * reference's SOS leaves in channel 0 (ImageFilter.cpp:163-166). */
+int fr_real_to_complex(const float *d_in, size_t n, float *d_out, void *stream);
+
+/* PILS image operations (Program/Main.cpp:131-164), on channel images in
+ * place, with the reference's float arithmetic:
+ *   fr_low_filter  : ImageFilter::lowFilter(res)  (ImageFilter.cpp:55-93)
+ *   fr_normalize_channels : ImageFilter::normalize (ImageFilter.cpp:95-118)
+ *   fr_sos_map     : ImageFilter::SOS(map, reconSize) (ImageFilter.cpp:170-209),
+ *                    sum over channels of x * conj(map) over the centred crop,
+ *                    complex output (recon size), no square root. */
+int fr_low_filter(float *d_imgs, int channels, int dim, const unsigned *size, int res, void *stream);
+int fr_normalize_channels(float *d_imgs, int channels, int dim, const unsigned *size, void *stream);
+int fr_sos_map(const float *d_imgs, const float *d_maps, int channels, int dim, const unsigned *size,
+               const unsigned *recon, float *d_out, void *stream);
 
 /* ------------------------------------------------------------------------
  * Whole reconstruction (Program/Main.cpp:101-181 without file I/O):

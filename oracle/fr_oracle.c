@@ -488,6 +488,83 @@ void orc_sos(const float *imgs, int channels, int dim, const unsigned *size,
     }
 }
 
+/* ImageFilter::lowFilter, ImageFilter.cpp:55-93. */
+void orc_low_filter(float *imgs, int channels, int dim, const unsigned *size, int res)
+{
+    unsigned sx = size[0], sy = size[1], sz = dim == 3 ? size[2] : 1;
+    long long x0 = sx / 2, y0 = sy / 2, z0 = sz / 2;
+    float att = (float)(2.0 * res * res / 4.0);
+    float coeff[2000];
+    for (int r = 0; r < 2000; r++)
+        coeff[r] = expf((float)(-r / 100.0));
+    size_t cells = (size_t)sx * sy * sz;
+    for (int c = 0; c < channels; ++c) {
+        float *d = imgs + 2 * cells * (size_t)c;
+        size_t o = 0;
+        for (long long z = 0; z < sz; z++) {
+            int r1 = (int)((z - z0) * (z - z0));
+            for (long long y = 0; y < sy; y++) {
+                int r2 = (int)((y - y0) * (y - y0) + r1);
+                for (long long x = 0; x < sx; x++, o++) {
+                    int r = (int)((x - x0) * (x - x0) + r2);
+                    int idx = (int)((double)((float)r / att) * 100.0);
+                    if (idx >= 2000) {
+                        d[2 * o] = 0;
+                        d[2 * o + 1] = 0;
+                    } else {
+                        d[2 * o] = d[2 * o] * coeff[idx];
+                        d[2 * o + 1] = d[2 * o + 1] * coeff[idx];
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* ImageFilter::normalize, ImageFilter.cpp:95-118 (std::norm is re*re + im*im). */
+void orc_normalize_channels(float *imgs, int channels, int dim, const unsigned *size)
+{
+    size_t cells = (size_t)size[0] * size[1] * (dim == 3 ? size[2] : 1);
+    for (size_t v = 0; v < cells; ++v) {
+        float mag = 0;
+        for (int c = 0; c < channels; ++c) {
+            float a = imgs[2 * (cells * c + v)], b = imgs[2 * (cells * c + v) + 1];
+            mag = mag + (a * a + b * b);
+        }
+        float s = sqrtf(mag);
+        for (int c = 0; c < channels; ++c) {
+            imgs[2 * (cells * c + v)] = imgs[2 * (cells * c + v)] / s;
+            imgs[2 * (cells * c + v) + 1] = imgs[2 * (cells * c + v) + 1] / s;
+        }
+    }
+}
+
+/* ImageFilter::SOS(map, reconSize), ImageFilter.cpp:170-209. */
+void orc_sos_map(const float *imgs, const float *maps, int channels, int dim, const unsigned *size,
+                 const unsigned *recon, float *out)
+{
+    unsigned isx = size[0], isy = size[1], isz = dim == 3 ? size[2] : 1;
+    unsigned rsx = recon[0], rsy = recon[1], rsz = dim == 3 ? recon[2] : 1;
+    unsigned x0 = (isx - rsx) / 2, y0 = (isy - rsy) / 2, z0 = (isz - rsz) / 2;
+    size_t nout = (size_t)rsx * rsy * rsz, cells = (size_t)isx * isy * isz;
+    memset(out, 0, nout * 2 * sizeof(float));
+    for (int c = 0; c < channels; ++c) {
+        const float *img = imgs + 2 * cells * (size_t)c, *map = maps + 2 * cells * (size_t)c;
+        for (unsigned z = 0; z < rsz; z++)
+            for (unsigned y = 0; y < rsy; y++)
+                for (unsigned x = 0; x < rsx; x++) {
+                    size_t in3 = ((size_t)(z + z0) * isy + (y + y0)) * isx + (x + x0);
+                    size_t out3 = ((size_t)z * rsy + y) * rsx + x;
+                    float a = img[2 * in3], b = img[2 * in3 + 1];
+                    float cr = map[2 * in3], nd = -map[2 * in3 + 1];
+                    float re = a * cr - b * nd;
+                    float im = a * nd + b * cr;
+                    out[2 * out3] = out[2 * out3] + re;
+                    out[2 * out3 + 1] = out[2 * out3 + 1] + im;
+                }
+    }
+}
+
 /* Program/Main.cpp:101-181 without file I/O. */
 int orc_recon(float *traj, const float *dcf, const float *kdata, size_t n, int channels,
               int dim, unsigned reconSize, float os, float kWidth, int klength,

@@ -104,6 +104,16 @@ void orc_fft_shift(float *data, int dim, const unsigned *size);
 void orc_sos(const float *imgs, int channels, int dim, const unsigned *size,
              const unsigned *recon, float *out);
 
+/* PILS operations, in place on `channels` images of `size`:
+ * ImageFilter::lowFilter(res) (ImageFilter.cpp:55-93), ImageFilter::normalize
+ * (ImageFilter.cpp:95-118).  orc_sos_map is ImageFilter::SOS(map, reconSize)
+ * (ImageFilter.cpp:170-209): centred crop, sum over channels of x*conj(map),
+ * complex output, no square root. */
+void orc_low_filter(float *imgs, int channels, int dim, const unsigned *size, int res);
+void orc_normalize_channels(float *imgs, int channels, int dim, const unsigned *size);
+void orc_sos_map(const float *imgs, const float *maps, int channels, int dim, const unsigned *size,
+                 const unsigned *recon, float *out);
+
 /* The whole reference pipeline (Program/Main.cpp:101-181) without I/O:
  * normalizeTraj, grid, backward FFT, fftShift, SOS, |.| -> float image.
  * traj is modified in place (as the reference does).  Returns 0 on success. */

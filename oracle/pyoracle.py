@@ -54,6 +54,9 @@ class Oracle:
         lib.orc_fft.argtypes = [_f32p, C.c_int, _u32p, C.c_int, C.c_int, C.c_int]
         lib.orc_fft_shift.argtypes = [_f32p, C.c_int, _u32p]
         lib.orc_sos.argtypes = [_f32p, C.c_int, C.c_int, _u32p, _u32p, _f32p]
+        lib.orc_low_filter.argtypes = [_f32p, C.c_int, C.c_int, _u32p, C.c_int]
+        lib.orc_normalize_channels.argtypes = [_f32p, C.c_int, C.c_int, _u32p]
+        lib.orc_sos_map.argtypes = [_f32p, _f32p, C.c_int, C.c_int, _u32p, _u32p, _f32p]
         lib.orc_recon.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_int, C.c_uint,
                                   C.c_float, C.c_float, C.c_int, _u32p, _f32p, C.c_int]
 
@@ -149,6 +152,28 @@ class Oracle:
         self.lib.orc_sos(a.view(np.float32).ravel(), a.shape[0], dim, size, rec, out.view(np.float32))
         return out
 
+    def low_filter(self, imgs, dim, G, res):
+        a = np.array(imgs, np.complex64, copy=True, order="C")
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        self.lib.orc_low_filter(a.view(np.float32).ravel(), a.shape[0], dim, size, res)
+        return a
+
+    def normalize_channels(self, imgs, dim, G):
+        a = np.array(imgs, np.complex64, copy=True, order="C")
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        self.lib.orc_normalize_channels(a.view(np.float32).ravel(), a.shape[0], dim, size)
+        return a
+
+    def sos_map(self, imgs, maps, dim, G, recon):
+        a = np.ascontiguousarray(imgs, np.complex64)
+        m = np.ascontiguousarray(maps, np.complex64)
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.complex64)
+        self.lib.orc_sos_map(a.view(np.float32).ravel(), m.view(np.float32).ravel(), a.shape[0], dim, size, rec,
+                             out.view(np.float32))
+        return out
+
     def recon(self, traj4, dcf, kdata, dim, reconSize, os_, W, L, recon, threads=1) -> np.ndarray:
         t = np.array(traj4, np.float32, copy=True, order="C")
         kd = np.ascontiguousarray(kdata, np.complex64)
@@ -173,6 +198,10 @@ class RefLib:
         lib.ref_grid.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
                                  C.c_float, C.c_float, C.c_uint, C.c_int, _f32p, _f32p]
         lib.ref_shift_sos.argtypes = [_f32p, C.c_int, C.c_int, C.c_uint, _u32p, _f32p]
+        lib.ref_pils_op.argtypes = [C.c_int, _f32p, C.c_void_p, C.c_int, C.c_int, C.c_uint, C.c_int, _u32p,
+                                    C.c_void_p]
+        lib.ref_recon_pils.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                       C.c_float, C.c_float, C.c_uint, C.c_int, _u32p, _f32p]
         lib.ref_recon.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
                                   C.c_float, C.c_float, C.c_uint, C.c_int, _u32p, _f32p]
 
@@ -200,6 +229,24 @@ class RefLib:
         rec = np.array(recon, np.uint32)
         out = np.zeros(int(np.prod(rec)), np.complex64)
         self.lib.ref_shift_sos(a.view(np.float32).ravel(), a.shape[0], dim, G, rec, out.view(np.float32))
+        return out
+
+    def pils_op(self, op, imgs, dim, G, res=22, maps=None, recon=(1, 1, 1)):
+        a = np.array(imgs, np.complex64, copy=True, order="C")
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.complex64)
+        m = np.ascontiguousarray(maps, np.complex64) if maps is not None else None
+        self.lib.ref_pils_op(op, a.view(np.float32).ravel(), m.ctypes.data if m is not None else None, a.shape[0],
+                             dim, G, res, rec, out.ctypes.data)
+        return out if op == 2 else a
+
+    def recon_pils(self, traj4, dcf, kdata, samples, acquisitions, dim, reconSize, os_, W, L, recon, threads=1):
+        kd = np.ascontiguousarray(kdata, np.complex64)
+        rec = np.array(recon, np.uint32)
+        out = np.zeros(int(np.prod(rec)), np.float32)
+        self.lib.ref_recon_pils(np.ascontiguousarray(traj4, np.float32), np.ascontiguousarray(dcf, np.float32),
+                                kd.view(np.float32).ravel(), samples, acquisitions, dim, kd.shape[0], reconSize,
+                                os_, W, L, threads, rec, out)
         return out
 
     def recon(self, traj4, dcf, kdata, samples, acquisitions, dim, reconSize, os_, W, L, recon, threads=1):

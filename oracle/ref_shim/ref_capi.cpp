@@ -92,6 +92,70 @@ extern "C" int ref_shift_sos(const float *imgs, int channels, int dim, unsigned 
     return 0;
 }
 
+// ImageFilter::lowFilter / normalize / SOS(map) on channel images.
+// op: 0 = lowFilter(res), 1 = normalize, 2 = SOS(map, recon) (out = complex recon image)
+extern "C" int ref_pils_op(int op, float *imgs, const float *maps, int channels, int dim, unsigned G, int res,
+                           const unsigned *recon, float *out)
+{
+    ImageSize sz = {G, G, G};
+    ImageData<float> img(dim, sz), map(dim, sz);
+    size_t cells = img.dataSize();
+    for (int c = 0; c < channels; ++c) {
+        ComplexVector<float> v(cells);
+        std::memcpy(v.data(), imgs + 2 * cells * (size_t)c, cells * sizeof(std::complex<float>));
+        img.addChannelImage(std::move(v));
+        if (maps) {
+            ComplexVector<float> m(cells);
+            std::memcpy(m.data(), maps + 2 * cells * (size_t)c, cells * sizeof(std::complex<float>));
+            map.addChannelImage(std::move(m));
+        }
+    }
+    auto filter = ImageFilter<float>::Create(img);
+    if (op == 0 || op == 1) {
+        if (op == 0)
+            filter->lowFilter(res);
+        else
+            filter->normalize();
+        for (int c = 0; c < channels; ++c)
+            std::memcpy(imgs + 2 * cells * (size_t)c, img.getChannelImage(c)->data(),
+                        cells * sizeof(std::complex<float>));
+        return 0;
+    }
+    filter->SOS(map, {recon[0], recon[1], recon[2]});
+    size_t nout = (size_t)recon[0] * recon[1] * recon[2];
+    std::memcpy(out, img.getChannelImage(0)->data(), nout * sizeof(std::complex<float>));
+    return 0;
+}
+
+// The PILS branch of Main.cpp:131-164 without I/O: |SOS(map)| float image.
+extern "C" int ref_recon_pils(const float *traj4, const float *dcf, const float *kdata, int samples,
+                              int acquisitions, int dim, int channels, unsigned reconSize, float os, float kWidth,
+                              unsigned klength, int threads, const unsigned *recon, float *out_mag)
+{
+    auto rd = load(traj4, dcf, kdata, samples, acquisitions, dim, channels);
+    auto grid = GridLut<float>::Create(*rd);
+    grid->setNumOfThreads(threads);
+    grid->plan(reconSize, os, kWidth, klength);
+    auto imgData = grid->execute();
+    ImageData<float> imgMap;
+    imgMap = *imgData;
+    auto filter = ImageFilter<float>::Create(*imgData);
+    filter->setNumOfThreads(threads);
+    filter->fftPlan();
+    filter->fftExecute();
+    filter->fftShift();
+    auto filterMap = ImageFilter<float>::Create(imgMap);
+    filterMap->lowFilter(22);
+    filterMap->fftExecute();
+    filterMap->fftShift();
+    filterMap->normalize();
+    filter->SOS(imgMap, {recon[0], recon[1], recon[2]});
+    size_t nout = (size_t)recon[0] * recon[1] * recon[2];
+    const auto *d = imgData->getChannelImage(0);
+    for (size_t i = 0; i < nout; ++i) out_mag[i] = std::abs((*d)[i]);
+    return 0;
+}
+
 // The whole CPU pipeline of Main.cpp:101-181 without I/O: |SOS| float image.
 extern "C" int ref_recon(const float *traj4, const float *dcf, const float *kdata, int samples,
                          int acquisitions, int dim, int channels, unsigned reconSize, float os,

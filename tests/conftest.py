@@ -11,7 +11,7 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 CASE_NAMES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                    if not p.endswith("luts.npz"))
+                    if not p.endswith(("luts.npz", "pils_ops.npz")))
 
 
 def pytest_configure(config):

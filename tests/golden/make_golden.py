@@ -63,12 +63,28 @@ def main():
         grid, tn = ref.grid(traj, dcf, kd, b, a, dim, recon, os_, W, L, threads=2)
         rec = (recon, recon, recon if dim == 3 else 1)
         img = ref.recon(traj, dcf, kd, b, a, dim, recon, os_, W, L, rec, threads=2)
+        img_pils = ref.recon_pils(traj, dcf, kd, b, a, dim, recon, os_, W, L, rec, threads=2)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), traj=traj, dcf=dcf, kdata=kd, traj_norm=tn,
-                            grid=grid, image=img, lut=ref.kb_lut(W, os_, L),
+                            grid=grid, image=img, image_pils=img_pils, lut=ref.kb_lut(W, os_, L),
                             params=np.array([dim, a, b, C, recon, os_, W, L, pw], np.float64))
         print(name, traj.shape, grid.shape, img.shape)
     luts = {f"w{w}_os{o}_l{l}": ref.kb_lut(w, o, l) for (w, o, l) in LUTS}
     np.savez_compressed(os.path.join(HERE, "luts.npz"), **luts)
+    # PILS image operations (ImageFilter::lowFilter / normalize / SOS(map)) on random images
+    rng = np.random.default_rng(7)
+    pils = {}
+    for dim, G in [(2, 40), (3, 12), (2, 31)]:
+        x = (rng.standard_normal((3, G ** dim)) + 1j * rng.standard_normal((3, G ** dim))).astype(np.complex64)
+        m = (rng.standard_normal((3, G ** dim)) + 1j * rng.standard_normal((3, G ** dim))).astype(np.complex64)
+        rec = (G // 2, G // 2, G // 2 if dim == 3 else 1)
+        key = f"d{dim}_g{G}"
+        pils[key + "_in"] = x
+        pils[key + "_map"] = m
+        pils[key + "_low22"] = ref.pils_op(0, x, dim, G, 22)
+        pils[key + "_low5"] = ref.pils_op(0, x, dim, G, 5)
+        pils[key + "_norm"] = ref.pils_op(1, x, dim, G)
+        pils[key + "_sosmap"] = ref.pils_op(2, x, dim, G, maps=m, recon=rec)
+    np.savez_compressed(os.path.join(HERE, "pils_ops.npz"), **pils)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,86 @@
+"""The C++ drop-in API (include/fastrecon/*.h, libfastrecon.so): it builds and
+links on the CPU; on the GPU the Program/Main.cpp pipeline written against it
+(tests/cpp/recon_main.cpp, through ReconData::loadFromFiles, GridLut,
+ImageFilter) reproduces the reference's outputs, plain and PILS."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import CASE_NAMES, ROOT, load_case, rel_l2
+
+CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+LIBDIR = os.path.join(ROOT, "fastrecon_gb300", "_lib")
+
+
+def compile_main(outdir):
+    from fastrecon_gb300 import build
+    build.build()
+    exe = os.path.join(outdir, "recon_main")
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
+           os.path.join(ROOT, "tests", "cpp", "recon_main.cpp"), "-o", exe, "-L", LIBDIR, "-lfastrecon",
+           "-lfastrecon_gb300", "-L", os.path.join(CUDA, "lib64"), "-lcudart", f"-Wl,-rpath,{LIBDIR}",
+           f"-Wl,-rpath,{os.path.join(CUDA, 'lib64')}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_cpp_api_builds_and_links(tmp_path):
+    exe = compile_main(str(tmp_path))
+    assert os.path.exists(exe)
+    nm = subprocess.run(["nm", "-DC", os.path.join(LIBDIR, "libfastrecon.so")], capture_output=True, text=True).stdout
+    for sym in ["ReconData<float>::Create", "ReconData<float>::loadFromFiles", "ReconData<float>::normalizeTraj",
+                "GridLut<float>::Create", "cuGridLut<float>::plan", "cuGridLut<float>::execute",
+                "ConvKernel::ConvKernel", "ImageFilter<float>::Create", "ImageFilter<float>::SOS",
+                "ImageFilter<float>::fftShift", "ImageFilter<float>::lowFilter", "ImageFilter<float>::normalize",
+                "ImageFilter<float>::crop", "cuImageData<float>::cuGetChannelImage", "ImageData<float>::addChannelImage"]:
+        assert sym in nm, sym
+
+
+def write_case(c, d):
+    dim = c["dim"]
+    for k in range(dim):
+        np.ascontiguousarray(c["traj"][:, k]).astype(np.float32).tofile(os.path.join(d, f"traj_{k}.f32"))
+    c["dcf"].astype(np.float32).tofile(os.path.join(d, "dcf.f32"))
+    for ch in range(c["coils"]):
+        np.ascontiguousarray(c["kdata"][ch]).astype(np.complex64).tofile(os.path.join(d, f"data_{ch}.c64"))
+
+
+def run_main(exe, c, d, pils=False):
+    rz = c["recon"] if c["dim"] == 3 else 1
+    args = [exe, d, str(c["readout"]), str(c["spokes"]), str(c["coils"]), str(c["dim"]), str(c["recon"]),
+            str(c["recon"]), str(rz), repr(c["os"]), repr(c["W"]), str(c["L"])] + (["pils"] if pils else [])
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = np.fromfile(os.path.join(d, "out.f32"), np.float32)
+    tn = np.fromfile(os.path.join(d, "traj_norm.f32"), np.float32).reshape(-1, 4)
+    g0 = np.fromfile(os.path.join(d, "grid0.c64"), np.complex64)
+    return out, tn, g0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_main_pipeline_vs_reference(tmp_path, name):
+    c = load_case(name)
+    exe = compile_main(str(tmp_path))
+    write_case(c, str(tmp_path))
+    out, tn, g0 = run_main(exe, c, str(tmp_path))
+    assert np.array_equal(tn.view(np.uint32), c["traj_norm"].view(np.uint32))
+    assert rel_l2(g0, c["grid"][0]) <= 1e-5
+    err = rel_l2(out, c["image"])
+    print(f"{name}: C++ API recon rel-L2 vs reference {err:.2e}")
+    assert err <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small", "radial2d_oddgrid"])
+def test_main_pipeline_pils_vs_reference(tmp_path, name):
+    c = load_case(name)
+    exe = compile_main(str(tmp_path))
+    write_case(c, str(tmp_path))
+    out, _, _ = run_main(exe, c, str(tmp_path), pils=True)
+    err = rel_l2(out, c["image_pils"])
+    print(f"{name}: C++ API PILS recon rel-L2 vs reference {err:.2e}")
+    assert err <= 1e-5

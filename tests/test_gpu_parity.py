@@ -329,3 +329,29 @@ def test_deapodization_flattens_point_response(torch):
     b = raw.run(cu(torch, t), cu(torch, dcf), cu(torch, kd)).cpu().numpy().reshape(64, 64)
     assert b[32, 32] > 1.2 * b[32, 0] and b[32, 32] > 1.2 * b[0, 0]  # apodized
     assert np.max(np.abs(a / a[32, 32] - 1)) < 1e-3
+
+
+# ----------------------------------------------------------------- PILS ----
+
+def test_pils_ops_bit_exact(torch):
+    """lowFilter / normalize / SOS(map) kernels against the reference's own
+    ImageFilter outputs (tests/golden/pils_ops.npz), bit for bit."""
+    import os
+    import fastrecon_gb300 as fr
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "pils_ops.npz"))
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files if k.endswith("_in")})
+    for key in keys:
+        dim, G = int(key.split("_")[0][1:]), int(key.split("_")[1][1:])
+        x = z[key + "_in"]
+        for res in (22, 5):
+            xd = cu(torch, x)
+            fr.gridding.low_filter(xd, dim, G, res)
+            assert np.array_equal(bits(xd.cpu().numpy().view(np.float32)),
+                                  bits(z[f"{key}_low{res}"].view(np.float32))), key
+        xd = cu(torch, x)
+        fr.gridding.normalize_channels(xd, dim, G)
+        assert np.array_equal(bits(xd.cpu().numpy().view(np.float32)), bits(z[key + "_norm"].view(np.float32))), key
+        rec = (G // 2, G // 2, G // 2 if dim == 3 else 1)
+        out = fr.gridding.sos_map(cu(torch, x), cu(torch, z[key + "_map"]), dim, G, rec).cpu().numpy()
+        assert np.array_equal(bits(out.view(np.float32)), bits(z[key + "_sosmap"].view(np.float32))), key

@@ -104,3 +104,24 @@ def test_oracle_vs_reference_random(oracle):
         assert np.array_equal(bits(tn), bits(tn_ref))
         g = oracle.grid(tn, dcf, kd, dim, 18, 4.0, oracle.kb_lut(4.0, 1.5, 512))
         assert np.array_equal(bits(g.view(np.float32)), bits(g_ref.view(np.float32)))
+
+
+def _pils_cases():
+    z = np.load(os.path.join(GOLDEN, "pils_ops.npz"))
+    for key in sorted({k.rsplit("_", 1)[0] for k in z.files if k.endswith("_in")}):
+        dim, G = int(key.split("_")[0][1:]), int(key.split("_")[1][1:])
+        yield key, dim, G, z
+
+
+def test_pils_ops_bit_exact(oracle):
+    """ImageFilter::lowFilter / normalize / SOS(map) restated bit-for-bit."""
+    for key, dim, G, z in _pils_cases():
+        x = z[key + "_in"]
+        for res in (22, 5):
+            assert np.array_equal(bits(oracle.low_filter(x, dim, G, res).view(np.float32)),
+                                  bits(z[f"{key}_low{res}"].view(np.float32))), key
+        assert np.array_equal(bits(oracle.normalize_channels(x, dim, G).view(np.float32)),
+                              bits(z[key + "_norm"].view(np.float32))), key
+        rec = (G // 2, G // 2, G // 2 if dim == 3 else 1)
+        got = oracle.sos_map(x, z[key + "_map"], dim, G, rec)
+        assert np.array_equal(bits(got.view(np.float32)), bits(z[key + "_sosmap"].view(np.float32))), key
