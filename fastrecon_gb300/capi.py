@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libfastrecon_gb300.so")
 
 FR_PLAN_CHECKERBOARD = 1
 FR_RECON_DEAPODIZE = 1
+FR_RECON_CUFFT = 2
 
 _lib = None
 
@@ -44,6 +45,8 @@ _SIGS = {
     "fr_last_error": (C.c_char_p, []),
     "fr_version": (C.c_char_p, []),
     "fr_kb_lut": (C.c_int, [C.c_float, C.c_float, C.c_int, C.POINTER(C.c_float)]),
+    "fr_lut_index_table": (C.c_int, [C.c_float, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float)]),
     "fr_plan_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(_VP)]),
     "fr_plan_destroy": (C.c_int, [_VP]),
     "fr_plan_set_trajectory": (C.c_int, [_VP, _VP, C.c_size_t, _VP]),
@@ -61,6 +64,9 @@ _SIGS = {
     "fr_fft_create": (C.c_int, [C.c_int, C.POINTER(C.c_uint), C.c_int, C.c_int, C.POINTER(_VP)]),
     "fr_fft_execute": (C.c_int, [_VP, _VP, _VP]),
     "fr_fft_destroy": (C.c_int, [_VP]),
+    "fr_fft_crop_sos_create": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.POINTER(C.c_uint), C.POINTER(_VP)]),
+    "fr_fft_crop_sos_execute": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+    "fr_fft_crop_sos_destroy": (C.c_int, [_VP]),
     "fr_fft_shift": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), _VP]),
     "fr_crop": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), _VP, _VP]),
     "fr_sos": (C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint), _VP, _VP, _VP]),

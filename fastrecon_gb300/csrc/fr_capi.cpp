@@ -70,6 +70,61 @@ static double bessel_i0(double x)
     return sum;
 }
 
+// GridLut.cpp:131-136 on the host: dk = sqrtf(s), valid iff dk < kHW,
+// index roundf(dk / kHW * (L-1)).  volatile keeps each float rounding.
+int lut_reference_index(float s, float hw, int L)
+{
+    volatile float dk = std::sqrt(s);
+    if (!(dk < hw)) return -1;
+    volatile float q = dk / hw;
+    volatile float t = q * (float)(L - 1);
+    return (int)std::round((float)t);
+}
+
+static inline unsigned fbits(float f)
+{
+    unsigned u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+static inline float bitsf(unsigned u)
+{
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+LutIndexTable lut_index_table(float hw, int L)
+{
+    LutIndexTable t;
+    // non-negative floats are ordered like their bit patterns
+    unsigned lo = 0, hi = fbits(std::max(4.f * hw * hw, 1.f));
+    while (lo < hi) {  // smallest s with !(sqrtf(s) < hw)
+        unsigned mid = lo + (hi - lo) / 2;
+        if (lut_reference_index(bitsf(mid), hw, L) < 0)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    t.smax = bitsf(lo);
+    const unsigned top = lo;  // all valid s are below bitsf(top)
+    t.thr.assign(L + 1, INFINITY);
+    t.thr[0] = 0.f;
+    for (int k = 1; k < L; ++k) {
+        unsigned a = 0, b = top;  // smallest s < smax with ki(s) >= k, else +inf
+        while (a < b) {
+            unsigned mid = a + (b - a) / 2;
+            if (lut_reference_index(bitsf(mid), hw, L) >= k)
+                b = mid;
+            else
+                a = mid + 1;
+        }
+        t.thr[k] = a < top ? bitsf(a) : INFINITY;
+    }
+    t.kc = (float)(L - 1) / hw;
+    return t;
+}
+
 }  // namespace fr
 
 fr_plan_s::~fr_plan_s()
@@ -119,6 +174,17 @@ int fr_kb_lut(float kWidth, float overGridFactor, int length, float *out)
         if (i == 0) kernel0 = out[0];
         out[i] = out[i] / kernel0;
     }
+    return FR_OK;
+}
+
+int fr_lut_index_table(float kernel_width, int length, float *thresholds, float *smax, float *kc)
+{
+    if (!(kernel_width > 0.f) || length < 2 || !thresholds)
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad lut index table arguments");
+    LutIndexTable t = lut_index_table(kernel_width / 2, length);
+    std::memcpy(thresholds, t.thr.data(), sizeof(float) * (length + 1));
+    if (smax) *smax = t.smax;
+    if (kc) *kc = t.kc;
     return FR_OK;
 }
 
@@ -184,11 +250,26 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         float h2 = p->hw * p->hw;
         p->prefilter = (std::sqrt(h2) == p->hw) && ((double)h2 == (double)p->hw * (double)p->hw);
     }
-    if (p->lut_d.reserve((size_t)p->L * 4)) {
+    // Device LUT entries {thr[k+1], lut[k], lut[k+1], 0}: the exact LUT
+    // index and weight from s = dk^2 without a square root (LutIndexTable).
+    {
+        LutIndexTable lt = lut_index_table(p->hw, p->L);
+        p->lut_smax = lt.smax;
+        p->lut_kc = lt.kc;
+        p->lut_entries.resize(4 * (size_t)p->L);
+        for (int k = 0; k < p->L; ++k) {
+            p->lut_entries[4 * k + 0] = lt.thr[k + 1];
+            p->lut_entries[4 * k + 1] = p->lut[k];
+            p->lut_entries[4 * k + 2] = k + 1 < p->L ? p->lut[k + 1] : 0.f;
+            p->lut_entries[4 * k + 3] = 0.f;
+        }
+    }
+    if (p->lut_d.reserve((size_t)p->L * 4) || p->lut_e.reserve((size_t)p->L * 16)) {
         delete p;
         return FR_ERR_OUT_OF_MEMORY;
     }
-    cudaError_t e = cudaMemcpy(p->lut_d.ptr, p->lut.data(), (size_t)p->L * 4, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(p->lut_e.ptr, p->lut_entries.data(), (size_t)p->L * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->lut_d.ptr, p->lut.data(), (size_t)p->L * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         delete p;
         return cuda_fail(e, "lut upload");

@@ -1,0 +1,397 @@
+// fr_fft.cu -- pruned backward FFT with fused crop and multi-coil sum of
+// squares.
+//
+// Replaces cuFFT::excute + fftShift + crop + SOS (cuFFT.cpp:24-37,
+// ImageFilter.cpp:40-53,159-209) when the grid was flushed with the
+// (-1)^(x+y+z) modulation (even G), so the transform output is already
+// shifted.  Only the centred out_size crop of the image is kept, so each of
+// the d one-dimensional stages keeps only the cropped outputs of its axis:
+//   x stage: lines along x of the grid          -> [C][Gz][Gy][Rx]
+//   y stage: lines along y                      -> [C][Gz][Ry][Rx]
+//   z stage: lines along z, all coils of a column in turn, |X|^2 summed over
+//            coils in coil order, sqrt (and / deapod)  -> [Rz][Ry][Rx]
+// (in 2D the y stage is the last one).  Each line is transformed in shared
+// memory by a self-sorting (Stockham) mixed-radix FFT with radix 2, 3, 4, 5
+// and 8 passes and a double-precision twiddle table rounded to float.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "fr_internal.h"
+
+namespace fr {
+namespace {
+
+constexpr int kMaxPasses = 12;
+constexpr int kMaxN = 1024;
+
+struct FftPlan1D {
+    int n;
+    int npass;
+    int radix[kMaxPasses];
+};
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by +i
+__device__ __forceinline__ float2 cmuli(float2 a) { return make_float2(-a.y, a.x); }
+
+// In-register DFTs with kernel exp(+2 pi i r k / p) (backward transform).
+__device__ __forceinline__ void dft2(float2 *v)
+{
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+__device__ __forceinline__ void dft4(float2 *v)
+{
+    const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    const float2 a2 = cadd(v[1], v[3]), a3 = cmuli(csub(v[1], v[3]));
+    v[0] = cadd(a0, a2);
+    v[2] = csub(a0, a2);
+    v[1] = cadd(a1, a3);
+    v[3] = csub(a1, a3);
+}
+__device__ __forceinline__ void dft3(float2 *v)
+{
+    const float c = -0.5f, s = 0.86602540378443864676f;  // cos, sin of 2 pi / 3
+    const float2 t1 = cadd(v[1], v[2]);
+    const float2 d = csub(v[1], v[2]);
+    const float2 m = cadd(v[0], cscale(t1, c));
+    const float2 r = cmuli(cscale(d, s));
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(m, r);
+    v[2] = csub(m, r);
+}
+__device__ __forceinline__ void dft5(float2 *v)
+{
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;  // cos(2pi/5), cos(4pi/5)
+    const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;   // sin(2pi/5), sin(4pi/5)
+    const float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    const float2 t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    const float2 a = cadd(v[0], cadd(cscale(t1, c1), cscale(t2, c2)));
+    const float2 b = cmuli(cadd(cscale(t3, s1), cscale(t4, s2)));
+    const float2 c = cadd(v[0], cadd(cscale(t1, c2), cscale(t2, c1)));
+    const float2 d = cmuli(csub(cscale(t3, s2), cscale(t4, s1)));
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(a, b);
+    v[4] = csub(a, b);
+    v[2] = cadd(c, d);
+    v[3] = csub(c, d);
+}
+__device__ __forceinline__ void dft8(float2 *v)
+{
+    const float h = 0.70710678118654752440f;  // 1/sqrt(2)
+    float2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    dft4(e);
+    dft4(o);
+    // twiddles exp(+2 pi i k / 8), k = 0..3
+    const float2 o1 = make_float2(h * (o[1].x - o[1].y), h * (o[1].x + o[1].y));
+    const float2 o2 = cmuli(o[2]);
+    const float2 o3 = make_float2(-h * (o[3].x + o[3].y), h * (o[3].x - o[3].y));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);
+    v[7] = csub(e[3], o3);
+}
+
+template <int R>
+__device__ __forceinline__ void dft(float2 *v)
+{
+    if constexpr (R == 2) dft2(v);
+    if constexpr (R == 3) dft3(v);
+    if constexpr (R == 4) dft4(v);
+    if constexpr (R == 5) dft5(v);
+    if constexpr (R == 8) dft8(v);
+}
+
+// One Stockham pass of radix R over `lines` lines in shared memory:
+// for j < n/R: v[r] = in[j + r n/R] * W^(r (j mod ns) n/(ns R)), DFT_R,
+// out[(j/ns) ns R + (j mod ns) + r ns] = v[r].  Element e of line l sits at
+// buf + l * lstride + e * estride.
+template <int R>
+__device__ __forceinline__ void stockham_pass(const float2 *__restrict__ in, float2 *__restrict__ out, int n, int ns,
+                                              int lines, int lstride, int estride, const float2 *__restrict__ tw)
+{
+    const int m = n / R;
+    const int tstep = n / (ns * R);
+    for (int idx = threadIdx.x; idx < m * lines; idx += blockDim.x) {
+        const int l = idx / m, j = idx - l * m;
+        const int k = j % ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float2 a = in[l * lstride + (j + r * m) * estride];
+            if (r > 0 && k > 0) a = cmul(a, tw[(r * k * tstep) % n]);
+            v[r] = a;
+        }
+        dft<R>(v);
+        const int o = (j / ns) * ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[l * lstride + (o + r * ns) * estride] = v[r];
+    }
+}
+
+// Full transform of `lines` lines held in buf0 (result in buf0 or buf1;
+// returns the buffer holding it).
+__device__ float2 *line_fft(float2 *buf0, float2 *buf1, const FftPlan1D &pl, int lines, int lstride, int estride,
+                            const float2 *tw)
+{
+    float2 *in = buf0, *out = buf1;
+    int ns = 1;
+    for (int p = 0; p < pl.npass; ++p) {
+        const int R = pl.radix[p];
+        switch (R) {
+        case 2: stockham_pass<2>(in, out, pl.n, ns, lines, lstride, estride, tw); break;
+        case 3: stockham_pass<3>(in, out, pl.n, ns, lines, lstride, estride, tw); break;
+        case 4: stockham_pass<4>(in, out, pl.n, ns, lines, lstride, estride, tw); break;
+        case 5: stockham_pass<5>(in, out, pl.n, ns, lines, lstride, estride, tw); break;
+        default: stockham_pass<8>(in, out, pl.n, ns, lines, lstride, estride, tw); break;
+        }
+        __syncthreads();
+        ns *= R;
+        float2 *t = in;
+        in = out;
+        out = t;
+    }
+    return in;
+}
+
+// x stage: LINES consecutive lines of length n (contiguous) per CTA, keep
+// outputs [x0, x0 + rx).  in: nlines x n, out: nlines x rx.
+__global__ void __launch_bounds__(256) fft_x_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                    long long nlines, FftPlan1D pl, int x0, int rx,
+                                                    const float2 *__restrict__ tw_g, int lines_per_cta)
+{
+    extern __shared__ float2 sm[];
+    const int n = pl.n;
+    float2 *tw = sm;
+    float2 *b0 = tw + n;
+    const int lstride = n + 1;  // pad against bank conflicts
+    float2 *b1 = b0 + lines_per_cta * lstride;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+    const long long l0 = (long long)blockIdx.x * lines_per_cta;
+    const int lines = (int)min((long long)lines_per_cta, nlines - l0);
+    for (int i = threadIdx.x; i < lines * n; i += blockDim.x) {
+        const int l = i / n, e = i - l * n;
+        b0[l * lstride + e] = in[(l0 + l) * n + e];
+    }
+    __syncthreads();
+    float2 *res = line_fft(b0, b1, pl, lines, lstride, 1, tw);
+    for (int i = threadIdx.x; i < lines * rx; i += blockDim.x) {
+        const int l = i / rx, e = i - l * rx;
+        out[(l0 + l) * rx + e] = res[l * lstride + x0 + e];
+    }
+}
+
+// Column stage: for each (outer, column block of COLS) transform the lines
+// along an axis of length n with element stride `stride` (in elements of the
+// input), keep outputs [y0, y0 + ry).  Input index: base(outer) + e*stride + c.
+// If `sos_out` is given this is the last stage: |X|^2 is summed over `coils`
+// consecutive inputs (coil stride `cstride`), then sqrt (/ deapod).
+constexpr int kCols = 16;
+
+__global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                      FftPlan1D pl, int y0, int ry, int ncols, long long stride,
+                                                      long long in_outer_stride, long long out_outer_stride,
+                                                      long long out_stride, const float2 *__restrict__ tw_g,
+                                                      int coils, long long cstride, float *__restrict__ sos_out,
+                                                      const float *__restrict__ deapod)
+{
+    extern __shared__ float2 sm[];
+    const int n = pl.n;
+    float2 *tw = sm;
+    float2 *b0 = tw + n;
+    float2 *b1 = b0 + n * kCols;
+    float *acc = reinterpret_cast<float *>(b1 + n * kCols);  // [ry][kCols] for the SoS stage
+    for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = tw_g[i];
+    const int cblocks = (ncols + kCols - 1) / kCols;
+    const long long outer = blockIdx.x / cblocks;
+    const int c0 = (blockIdx.x % cblocks) * kCols;
+    const int cw = min(kCols, ncols - c0);
+    if (sos_out)
+        for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) acc[i] = 0.f;
+    for (int coil = 0; coil < (sos_out ? coils : 1); ++coil) {
+        const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n * kCols; i += blockDim.x) {
+            const int e = i / kCols, c = i - e * kCols;
+            b0[i] = c < cw ? src[e * stride + c] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        // lines are columns: line stride 1, element stride kCols
+        float2 *res = line_fft(b0, b1, pl, kCols, 1, kCols, tw);
+        if (sos_out) {
+            for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) {
+                const int e = i / kCols, c = i - e * kCols;
+                const float2 v = res[(y0 + e) * kCols + c];
+                // x * conj(x) of the reference's SOS: re*re - im*(-im)
+                acc[i] = __fadd_rn(acc[i], __fsub_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, -v.y)));
+            }
+        } else {
+            float2 *dst = out + outer * out_outer_stride + c0;
+            for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) {
+                const int e = i / kCols, c = i - e * kCols;
+                if (c < cw) dst[e * out_stride + c] = res[(y0 + e) * kCols + c];
+            }
+        }
+    }
+    if (sos_out) {
+        __syncthreads();
+        float *dst = sos_out + outer * out_outer_stride + c0;
+        const float *dp = deapod ? deapod + outer * out_outer_stride + c0 : nullptr;
+        for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) {
+            const int e = i / kCols, c = i - e * kCols;
+            if (c < cw) {
+                float m = __fsqrt_rn(acc[i]);
+                if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                dst[e * out_stride + c] = m;
+            }
+        }
+    }
+}
+
+bool factor(int n, FftPlan1D &pl)
+{
+    pl.n = n;
+    pl.npass = 0;
+    int m = n;
+    const int radices[] = {8, 5, 4, 3, 2};
+    while (m > 1) {
+        bool ok = false;
+        for (int r : radices) {
+            if (m % r == 0) {
+                if (pl.npass >= kMaxPasses) return false;
+                pl.radix[pl.npass++] = r;
+                m /= r;
+                ok = true;
+                break;
+            }
+        }
+        if (!ok) return false;
+    }
+    return n >= 2 && n <= kMaxN;
+}
+
+}  // namespace
+}  // namespace fr
+
+using namespace fr;
+
+struct fr_fftcs_s {
+    int dim = 3;
+    unsigned G = 0;
+    int channels = 0;
+    unsigned out[3] = {0, 0, 0};
+    FftPlan1D pl;
+    DevBuf tw;    // G float2
+    DevBuf b1;    // x-stage output
+    DevBuf b2;    // y-stage output (3D)
+    int lines_x = 8;
+};
+
+extern "C" {
+
+int fr_fft_crop_sos_create(int dim, unsigned G, int channels, const unsigned *out_size, fr_fftcs *out)
+{
+    if (!out || !out_size || (dim != 2 && dim != 3) || channels < 1)
+        return fail(FR_ERR_INVALID_ARGUMENT, "bad pruned FFT arguments");
+    *out = nullptr;
+    auto f = new (std::nothrow) fr_fftcs_s;
+    if (!f) return fail(FR_ERR_OUT_OF_MEMORY, "pruned FFT");
+    f->dim = dim;
+    f->G = G;
+    f->channels = channels;
+    for (int i = 0; i < 3; ++i) f->out[i] = (i < dim) ? out_size[i] : 1u;
+    if (!factor((int)G, f->pl) || f->out[0] > G || f->out[1] > G || (dim == 3 && f->out[2] > G)) {
+        delete f;
+        return fail(FR_ERR_UNSUPPORTED, "pruned FFT needs G = 2^a 3^b 5^c <= 1024 and out_size <= G");
+    }
+    // exp(+2 pi i t / G) in double, rounded to float
+    std::vector<float2> tw(G);
+    for (unsigned t = 0; t < G; ++t) {
+        const double a = 2.0 * M_PI * (double)t / (double)G;
+        tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    const size_t Gz = dim == 3 ? G : 1;
+    if (f->tw.reserve(G * sizeof(float2)) ||
+        f->b1.reserve((size_t)channels * Gz * G * f->out[0] * sizeof(float2)) ||
+        (dim == 3 && f->b2.reserve((size_t)channels * G * f->out[1] * f->out[0] * sizeof(float2)))) {
+        delete f;
+        return FR_ERR_OUT_OF_MEMORY;
+    }
+    cudaError_t e = cudaMemcpy(f->tw.ptr, tw.data(), G * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete f;
+        return cuda_fail(e, "twiddle upload");
+    }
+    f->lines_x = 8;
+    *out = f;
+    return FR_OK;
+}
+
+int fr_fft_crop_sos_destroy(fr_fftcs f)
+{
+    delete f;
+    return FR_OK;
+}
+
+int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deapod, float *d_out, void *stream)
+{
+    if (!f || !d_grid || !d_out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int G = (int)f->G;
+    const int C = f->channels;
+    const int rx = f->out[0], ry = f->out[1], rz = f->out[2];
+    const int x0 = (G - rx) / 2, y0 = (G - ry) / 2, z0 = (G - rz) / 2;
+    const float2 *tw = f->tw.as<float2>();
+    const float2 *grid = reinterpret_cast<const float2 *>(d_grid);
+    float2 *b1 = f->b1.as<float2>();
+
+    // x stage over all lines of all coils
+    const long long Gz = f->dim == 3 ? G : 1;
+    const long long nl = (long long)C * Gz * G;
+    const int L = f->lines_x;
+    size_t smx = (size_t)(G + 2 * L * (G + 1)) * sizeof(float2);
+    if (smx > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(fft_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
+    fft_x_kernel<<<(unsigned)((nl + L - 1) / L), 256, smx, s>>>(grid, b1, nl, f->pl, x0, rx, tw, L);
+    FR_CHECK_LAUNCH("fft_x_kernel");
+
+    size_t smc = (size_t)(G + 2 * G * kCols) * sizeof(float2) + (size_t)G * kCols * sizeof(float);
+    if (smc > 48 * 1024)
+        FR_CUDA(cudaFuncSetAttribute(fft_col_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+    const int cblocks = (rx + kCols - 1) / kCols;
+    if (f->dim == 2) {
+        // y stage + SoS: outer = nothing (one plane), columns = x'
+        // input b1[c][y][x'] : element stride rx, coil stride G*rx
+        fft_col_kernel<<<cblocks, 256, smc, s>>>(b1, nullptr, f->pl, y0, ry, rx, rx, 0, 0, rx, tw, C,
+                                                 (long long)G * rx, d_out, d_deapod);
+        FR_CHECK_LAUNCH("fft_col_kernel(y, sos)");
+        return FR_OK;
+    }
+    // y stage: outer = (c, z), columns = x', input b1[c][z][y][x']
+    float2 *b2 = f->b2.as<float2>();
+    fft_col_kernel<<<(unsigned)((long long)C * G * cblocks), 256, smc, s>>>(
+        b1, b2, f->pl, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+    FR_CHECK_LAUNCH("fft_col_kernel(y)");
+    // z stage + SoS: outer = y', columns = x', input b2[c][z][y'][x'] with
+    // element (z) stride ry*rx, coil stride G*ry*rx; output out[z'][y'][x']
+    fft_col_kernel<<<(unsigned)((long long)ry * cblocks), 256, smc, s>>>(
+        b2, nullptr, f->pl, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C,
+        (long long)G * ry * rx, d_out, d_deapod);
+    FR_CHECK_LAUNCH("fft_col_kernel(z, sos)");
+    return FR_OK;
+}
+
+}  // extern "C"

@@ -33,7 +33,7 @@ struct GridParams {
     const SplitTile *splits;
     const float *kdata;  // channels x n complex64, as floats
     const float *dcf;
-    const float *lut;    // global copy, staged into shared memory
+    const float4 *lut_e; // {thr[k+1], lut[k], lut[k+1], 0}, staged into shared memory
     float *grid;         // channels x G^d complex64, as floats
     float *partials;     // nslots x ngroups x K x R floats
     long long n;
@@ -41,8 +41,8 @@ struct GridParams {
     int dim, G;
     int tile[3], ntile[3], K;
     int L;
-    float hw, inv_hw, lm1;
-    int hw_pow2, checkerboard;
+    float smax, kc, khalf;  // exact LUT index from s = dk^2 (LutIndexTable)
+    int checkerboard;
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -58,12 +58,63 @@ __device__ __forceinline__ int swz(int i)
     }
 }
 
+// Explicit shared-memory accesses on 32-bit shared addresses (generic
+// pointers would make every float atomic a run-time address-space dispatch).
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void red_add(unsigned a, float v)
+{
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ int4 lds_s32x4(unsigned a)
+{
+    int4 r;
+    asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "r"(a)
+                 : "memory");
+    return r;
+}
+__device__ __forceinline__ int2 lds_s32x2(unsigned a)
+{
+    int2 r;
+    asm volatile("ld.shared.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "r"(a) : "memory");
+    return r;
+}
+__device__ __forceinline__ float4 lds_f32x4(unsigned a)
+{
+    float4 r;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+                 : "r"(a)
+                 : "memory");
+    return r;
+}
+__device__ __forceinline__ float2 lds_f32x2(unsigned a)
+{
+    float2 r;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(a) : "memory");
+    return r;
+}
+__device__ __forceinline__ void sts_s32x2(unsigned a, int2 v)
+{
+    asm volatile("st.shared.v2.s32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
+}
+__device__ __forceinline__ unsigned lds_u8(unsigned a)
+{
+    unsigned r;
+    asm volatile("ld.shared.u8 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+    return r;
+}
+
 // Flush (or zero-fill) the tile's cells for one coil group.  Threads map to
-// (x, row) so consecutive lanes write consecutive x cells; row coordinates
-// advance incrementally (no divisions in the loop).
+// (x pair, row): each writes two consecutive x cells as one 16-byte store
+// (even tile x extent and grid size), rows advance without divisions.
 template <int R>
-__device__ __forceinline__ void write_cell_group(const GridParams &P, const float *acc, int cg, int ox,
-                                                 int oy, int oz, bool zero)
+__device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned acc, int cg, int ox, int oy, int oz,
+                                                 bool zero)
 {
     const int CG = P.coil_group;
     const int Tx = P.tile[0], Ty = P.tile[1], Tz = P.tile[2];
@@ -72,28 +123,37 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, const floa
     const int Gz = P.dim == 3 ? P.G : 1;
     const size_t cells = P.dim == 3 ? G * G * G : G * G;
     const int rows = Ty * Tz;
-    float2 *grid = reinterpret_cast<float2 *>(P.grid);
-    if ((int)blockDim.x % Tx == 0) {
-        const int lx = threadIdx.x % Tx, rr0 = threadIdx.x / Tx, rstep = blockDim.x / Tx;
+    const bool pairs = (Tx % 2 == 0) && (P.G % 2 == 0) && ((int)blockDim.x % (Tx / 2) == 0) &&
+                       ((reinterpret_cast<uintptr_t>(P.grid) & 15) == 0);
+    if (pairs) {
+        const int hx = Tx / 2;
+        const int lx = 2 * (threadIdx.x % hx), rr0 = threadIdx.x / hx, rstep = blockDim.x / hx;
         const int dy = rstep % Ty, dz = rstep / Ty;
         const int gx = ox + lx;
-        const bool xin = gx < P.G;
+        const bool xin = gx < P.G;  // gx even, G even: gx + 1 < G as well
         for (int cl = 0; cl < ncl; ++cl) {
-            const size_t cbase = (size_t)(cg * CG + cl) * cells;
+            float4 *gridc = reinterpret_cast<float4 *>(P.grid + 2 * (size_t)(cg * CG + cl) * cells);
             int ly = rr0 % Ty, lz = rr0 / Ty;
             for (int r = rr0; r < rows; r += rstep) {
                 const int gy = oy + ly, gz = oz + lz;
                 if (xin && gy < P.G && gz < Gz) {
-                    float2 v = make_float2(0.f, 0.f);
+                    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (!zero) {
                         const int i = r * Tx + lx;
-                        v = *reinterpret_cast<const float2 *>(acc + (size_t)i * R + ((2 * cl) ^ swz<R>(i)));
-                        if (P.checkerboard && ((gx + gy + gz) & 1)) {
-                            v.x = -v.x;
-                            v.y = -v.y;
+                        const float2 a = lds_f32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
+                        const float2 b = lds_f32x2(acc + 4u * (unsigned)((i + 1) * R + ((2 * cl) ^ swz<R>(i + 1))));
+                        v = make_float4(a.x, a.y, b.x, b.y);
+                        if (P.checkerboard) {  // (-1)^(x+y+z): opposite signs for x and x+1
+                            if ((gx + gy + gz) & 1) {
+                                v.x = -v.x;
+                                v.y = -v.y;
+                            } else {
+                                v.z = -v.z;
+                                v.w = -v.w;
+                            }
                         }
                     }
-                    grid[cbase + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+                    gridc[(((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1] = v;
                 }
                 ly += dy;
                 lz += dz;
@@ -106,6 +166,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, const floa
         return;
     }
     const int K = P.K;
+    float2 *grid = reinterpret_cast<float2 *>(P.grid);
     for (int idx = threadIdx.x; idx < ncl * K; idx += blockDim.x) {
         int cl = idx / K;
         int i = idx - cl * K;
@@ -117,7 +178,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, const floa
         if (gx >= P.G || gy >= P.G || gz >= Gz) continue;
         float2 v = make_float2(0.f, 0.f);
         if (!zero) {
-            v = *reinterpret_cast<const float2 *>(acc + (size_t)i * R + ((2 * cl) ^ swz<R>(i)));
+            v = lds_f32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
             if (P.checkerboard && ((gx + gy + gz) & 1)) {
                 v.x = -v.x;
                 v.y = -v.y;
@@ -134,14 +195,16 @@ template <int DIM, int R>
 __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
 {
     extern __shared__ float4 smem4[];
-    float *acc = reinterpret_cast<float *>(smem4);
     const int K = P.K;
-    float *lut = acc + (size_t)K * R;
-    // per warp, two buffers of a compacted tap list: {word offset of the
-    // tap's cell row (swizzled), weight}
-    int2 *lists = reinterpret_cast<int2 *>(lut + ((P.L + 3) & ~3));
-    // tap decode for boxes up to 4x4x4: dec[(nx-1)*4 + (ny-1)][t] = ix | iy<<2 | iz<<4
-    unsigned char *dec = reinterpret_cast<unsigned char *>(lists + kWarps * 2 * kListEntries);
+    // shared layout: accumulator tile [K][R] floats | LUT entries [L] float4 |
+    // per warp two tap-list buffers [32] {byte offset of the tap's cell row
+    // (swizzled), weight} | tap decode table [16][64] bytes
+    const unsigned acc = smem_addr(smem4);
+    const unsigned lutE = acc + (unsigned)K * R * 4u;
+    const unsigned lists = lutE + (unsigned)P.L * 16u;
+    const unsigned dec = lists + (unsigned)(kWarps * 2 * kListEntries * 8);
+    float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)K * R);
+    unsigned char *dec_g = reinterpret_cast<unsigned char *>(lutE_g + P.L) + kWarps * 2 * kListEntries * 8;
 
     const WorkItem it = P.items[blockIdx.x];
     const int cg = blockIdx.y;
@@ -157,11 +220,11 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
     }
 
     for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = threadIdx.x; i < P.L; i += blockDim.x) lut[i] = P.lut[i];
+    for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutE_g[i] = P.lut_e[i];
     for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
         const int nx = (i >> 8) + 1, ny = ((i >> 6) & 3) + 1, tt = i & 63;
         const int ix = tt % nx, iy = (tt / nx) % ny, iz = tt / (nx * ny);
-        dec[i] = (unsigned char)(ix | (iy << 2) | ((iz & 3) << 4));
+        dec_g[i] = (unsigned char)(ix | (iy << 2) | ((iz & 3) << 4));
     }
     __syncthreads();
 
@@ -172,10 +235,11 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
     constexpr int NF = R > 32 ? R / 32 : 1;   // floats per lane per tap
     const int q = R >= 32 ? 0 : lane / R;     // tap slot of this lane
     const int f0 = R >= 32 ? lane : lane % R; // first coil float of this lane
+    const unsigned f0b = (unsigned)f0 << 2;   // its byte offset in a cell row
     const int CG = P.coil_group;
     const int Tx = P.tile[0], Ty = P.tile[1];
-    int2 *mylist = lists + warp * 2 * kListEntries;
-    int buf = 0;
+    const unsigned mylist = lists + (unsigned)(warp * 2 * kListEntries * 8);
+    unsigned buf = 0;
 
     const float *kdf[NF];
     bool coil_ok[NF];
@@ -206,7 +270,7 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
         for (int k = 0; k < NF; ++k)
             val[k] = coil_ok[k] ? __fmul_rn(d, kdf[k][2 * (size_t)s]) : 0.f;  // GridLut.cpp:109
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
-        const unsigned char *dtab = dec + (((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64;
+        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64);
         const int nround = (ntap + 31) >> 5;
         for (int rnd = 0; rnd < nround; ++rnd) {
             const int tt = rnd * 32 + lane;
@@ -214,7 +278,7 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
             int ix = 0, iy = 0, iz = 0;
             if (ok) {
                 if (small) {
-                    const int code = dtab[tt];
+                    const unsigned code = lds_u8(dtab + tt);
                     ix = code & 3;
                     iy = (code >> 2) & 3;
                     iz = code >> 4;
@@ -231,44 +295,51 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
                 const float dx = __fsub_rn((float)(ox + lx), p.x);
                 const float dy = __fsub_rn((float)(oy + ly), p.y);
                 const float dz = DIM == 3 ? __fsub_rn((float)(oz + lz), p.z) : 0.f;
-                const int ki = tap_index(dx, __fmul_rn(dy, dy), __fmul_rn(dz, dz), P.hw, P.inv_hw, P.hw_pow2,
-                                         P.lm1, P.L);
-                ok = ki >= 0;
+                // GridLut.cpp:131: dk^2 = (dz^2 + dy^2) + dx^2, unfused
+                const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy)), __fmul_rn(dx, dx));
+                ok = s2 < P.smax;  // sqrtf(s2) < kHW
                 if (ok) {
+                    // first guess k0 in {ki-1, ki}, then one exact threshold test
+                    float a;
+                    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(s2));
+                    const int k0 = min((int)fmaf(a, P.kc, P.khalf), P.L - 1);
+                    const float4 en = lds_f32x4(lutE + 16u * (unsigned)k0);
+                    const float w = s2 >= en.x ? en.z : en.y;
                     const int cell = (lz * Ty + ly) * Tx + lx;
-                    e = make_int2(cell * R + swz<R>(cell), __float_as_int(lut[ki]));
+                    e = make_int2((cell * R + swz<R>(cell)) << 2, __float_as_int(w));
                 }
             }
             const unsigned m = __ballot_sync(0xffffffffu, ok);
             if (m == 0) continue;
-            int2 *lst = mylist + buf * kListEntries;
+            const unsigned lst = mylist + buf * (kListEntries * 8);
             buf ^= 1;
-            if (ok) lst[__popc(m & lt)] = e;
+            if (ok) sts_s32x2(lst + 8u * __popc(m & lt), e);
             __syncwarp();
             const int n = __popc(m);
             if (NG == 1) {
                 int k = 0;
                 for (; k + 1 < n; k += 2) {
-                    const int4 e2 = *reinterpret_cast<const int4 *>(lst + k);
+                    const int4 e2 = lds_s32x4(lst + 8u * k);
+                    const unsigned a0 = acc + ((unsigned)e2.x ^ f0b), a1 = acc + ((unsigned)e2.z ^ f0b);
 #pragma unroll
                     for (int kk = 0; kk < NF; ++kk) {
                         if (coil_ok[kk]) {
-                            atomicAdd(acc + ((e2.x ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e2.y), val[kk]));
-                            atomicAdd(acc + ((e2.z ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e2.w), val[kk]));
+                            red_add(a0 + 128u * kk, __fmul_rn(__int_as_float(e2.y), val[kk]));
+                            red_add(a1 + 128u * kk, __fmul_rn(__int_as_float(e2.w), val[kk]));
                         }
                     }
                 }
                 if (k < n) {
-                    const int2 e1 = lst[k];
+                    const int2 e1 = lds_s32x2(lst + 8u * k);
+                    const unsigned a0 = acc + ((unsigned)e1.x ^ f0b);
 #pragma unroll
                     for (int kk = 0; kk < NF; ++kk)
-                        if (coil_ok[kk])
-                            atomicAdd(acc + ((e1.x ^ f0) + 32 * kk), __fmul_rn(__int_as_float(e1.y), val[kk]));
+                        if (coil_ok[kk]) red_add(a0 + 128u * kk, __fmul_rn(__int_as_float(e1.y), val[kk]));
                 }
             } else {
                 for (int k = q; k < n; k += NG) {
-                    const int2 e1 = lst[k];
-                    if (coil_ok[0]) atomicAdd(acc + (e1.x ^ f0), __fmul_rn(__int_as_float(e1.y), val[0]));
+                    const int2 e1 = lds_s32x2(lst + 8u * k);
+                    if (coil_ok[0]) red_add(acc + ((unsigned)e1.x ^ f0b), __fmul_rn(__int_as_float(e1.y), val[0]));
                 }
             }
         }
@@ -365,7 +436,7 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
 size_t grid_smem_bytes(long long K, int R, int L)
 {
     // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode table
-    return (size_t)K * R * 4 + (size_t)((L + 3) & ~3) * 4 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64;
+    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64;
 }
 
 int floats_per_cell(int coil_group)
@@ -402,7 +473,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.splits = p->splits.as<SplitTile>();
     P.kdata = d_kdata;
     P.dcf = d_dcf;
-    P.lut = p->lut_d.as<float>();
+    P.lut_e = p->lut_e.as<float4>();
     P.grid = d_grid;
     P.n = (long long)p->n;
     P.channels = channels;
@@ -417,12 +488,9 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
         P.K *= p->tile[d];
     }
     P.L = p->L;
-    P.hw = p->hw;
-    int e;
-    float m = frexpf(p->hw, &e);
-    P.hw_pow2 = (m == 0.5f);
-    P.inv_hw = P.hw_pow2 ? ldexpf(1.0f, 1 - e) : 0.f;
-    P.lm1 = (float)(p->L - 1);
+    P.smax = p->lut_smax;
+    P.kc = p->lut_kc;
+    P.khalf = 0.25f;  // 0.5 - slack 0.25: the guess is the exact index or one below
     P.checkerboard = (p->flags & FR_PLAN_CHECKERBOARD) ? 1 : 0;
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;

@@ -85,6 +85,9 @@ struct fr_plan_s {
     float bounds_host[12] = {0};  // raw lo[3], raw hi[3], norm lo[3], norm hi[3]
 
     fr::DevBuf lut_d;         // L floats
+    fr::DevBuf lut_e;         // L float4 {thr[k+1], lut[k], lut[k+1], 0}
+    std::vector<float> lut_entries;
+    float lut_smax = 0.f, lut_kc = 0.f;
     fr::DevBuf traj;          // n float4, normalised
     fr::DevBuf bounds;        // 16 floats: raw lo/hi as ordered ints, tr, scale, norm lo/hi
     fr::DevBuf tile_count;    // ntiles int
@@ -122,6 +125,19 @@ int floats_per_cell(int coil_group);
 // Dynamic shared memory of the scatter kernel for K cells of R floats and an
 // L-entry LUT.
 size_t grid_smem_bytes(long long K, int R, int L);
+
+// Exact LUT index without a square root.  The reference index
+//   ki(s) = roundf(fl(fl(sqrtf(s)) / kHW) * (L-1)),  valid iff sqrtf(s) < kHW,
+// of s = dz^2 + dy^2 + dx^2 is a non-decreasing step function of s.
+// thr[k] (k = 1..L-1) is the smallest float s with ki(s) >= k, thr[L] = +inf,
+// and smax the smallest s with sqrtf(s) >= kHW.  Host computation, exact.
+struct LutIndexTable {
+    std::vector<float> thr;  // L + 1 entries, thr[0] = 0
+    float smax = 0.f;
+    float kc = 0.f;          // (L-1) / kHW for the approximate first guess
+};
+int lut_reference_index(float s, float hw, int L);  // the reference formula on the host (-1 if invalid)
+LutIndexTable lut_index_table(float hw, int L);
 }  // namespace fr
 
 namespace fr {

@@ -24,6 +24,7 @@ struct fr_recon_s {
     fr_plan plan = nullptr;
     fr_fft fft = nullptr;
     fr_fft fft1 = nullptr;  // single-image plan for the deapodization map
+    fr_fftcs pruned = nullptr;  // pruned FFT + crop + SoS (even G)
     DevBuf grid;            // channels x G^d complex
     DevBuf deapod;          // out_size floats
     DevBuf h_traj, h_dcf, h_kdata, h_img;  // device staging for host-buffer runs
@@ -36,6 +37,7 @@ struct fr_recon_s {
         if (plan) fr_plan_destroy(plan);
         if (fft) fr_fft_destroy(fft);
         if (fft1) fr_fft_destroy(fft1);
+        if (pruned) fr_fft_crop_sos_destroy(pruned);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -78,7 +80,12 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     }
     pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
     st = fr_plan_create(&pd, &r->plan);
-    if (!st) {
+    if (!st && r->checkerboard && !(d->flags & FR_RECON_CUFFT)) {
+        // the pruned transform where the grid size factors into 2, 3, 5
+        if (fr_fft_crop_sos_create(d->dim, r->G, d->channels, r->d.out_size, &r->pruned) != FR_OK)
+            r->pruned = nullptr;
+    }
+    if (!st && !r->pruned) {
         unsigned sz[3] = {r->G, r->G, d->dim == 3 ? r->G : 1u};
         st = fr_fft_create(d->dim, sz, d->channels, +1, &r->fft);
     }
@@ -140,12 +147,18 @@ int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const floa
     if (r->timing) cudaEventRecord(r->ev[1], s);
     if (!st) st = fr_grid(r->plan, d_kdata, d_dcf, r->d.channels, g, stream);
     if (r->timing) cudaEventRecord(r->ev[2], s);
-    if (!st) st = fr_fft_execute(r->fft, g, stream);
-    if (!st && !r->checkerboard) st = shift_run(g, r->d.channels, r->d.dim, sz, s);
-    if (r->timing) cudaEventRecord(r->ev[3], s);
-    if (!st)
-        st = sos_run(g, r->d.channels, r->d.dim, sz, r->d.out_size,
-                     (r->d.flags & FR_RECON_DEAPODIZE) ? r->deapod.as<float>() : nullptr, d_image, s);
+    const float *deapod = (r->d.flags & FR_RECON_DEAPODIZE) ? r->deapod.as<float>() : nullptr;
+    if (r->pruned) {
+        // transform, crop and SoS in one pruned pass (the stage times are
+        // reported as fft, with sos 0)
+        if (!st) st = fr_fft_crop_sos_execute(r->pruned, g, deapod, d_image, stream);
+        if (r->timing) cudaEventRecord(r->ev[3], s);
+    } else {
+        if (!st) st = fr_fft_execute(r->fft, g, stream);
+        if (!st && !r->checkerboard) st = shift_run(g, r->d.channels, r->d.dim, sz, s);
+        if (r->timing) cudaEventRecord(r->ev[3], s);
+        if (!st) st = sos_run(g, r->d.channels, r->d.dim, sz, r->d.out_size, deapod, d_image, s);
+    }
     if (r->timing) {
         cudaEventRecord(r->ev[4], s);
         cudaEventSynchronize(r->ev[4]);

@@ -234,12 +234,37 @@ def sos_map(imgs, maps, dim: int, G: int, recon, stream=None):
     return out
 
 
+class CropSoS:
+    """Pruned backward FFT + crop + SoS of a checkerboard-flushed grid
+    (fr_fft_crop_sos_*)."""
+
+    def __init__(self, dim: int, G: int, channels: int, out_size):
+        self.lib = capi.load()
+        self.out_size = tuple(list(out_size) + [1] * (3 - len(out_size)))
+        h = C.c_void_p()
+        check(self.lib.fr_fft_crop_sos_create(dim, G, channels, u3(self.out_size), C.byref(h)),
+              "fr_fft_crop_sos_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.fr_fft_crop_sos_destroy(self.h)
+            self.h = None
+
+    def __call__(self, grid, deapod=None, stream=None):
+        torch = _torch()
+        out = torch.empty(int(np.prod(self.out_size)), dtype=torch.float32, device="cuda")
+        check(self.lib.fr_fft_crop_sos_execute(self.h, _ptr(grid), _ptr(deapod), _ptr(out),
+                                               C.c_void_p(_stream(stream))), "fr_fft_crop_sos_execute")
+        return out
+
+
 class Recon:
     """The Program/Main.cpp pipeline as one object (fr_recon_*)."""
 
     def __init__(self, dim: int, recon_size: int, overgrid_factor: float, channels: int, out_size=None,
                  kernel_width: float = 4.0, lut_length: int = 512, max_samples: int = 0, tile=(0, 0, 0),
-                 coil_group: int = 0, deapodize: bool = False):
+                 coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False):
         self.lib = capi.load()
         d = capi.ReconDesc()
         d.dim = dim
@@ -255,7 +280,7 @@ class Recon:
         d.channels = channels
         d.max_samples = max_samples
         d.coil_group = coil_group
-        d.flags = capi.FR_RECON_DEAPODIZE if deapodize else 0
+        d.flags = (capi.FR_RECON_DEAPODIZE if deapodize else 0) | (capi.FR_RECON_CUFFT if use_cufft else 0)
         h = C.c_void_p()
         check(self.lib.fr_recon_create(C.byref(d), C.byref(h)), "fr_recon_create")
         self.h = h

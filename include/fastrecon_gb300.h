@@ -54,6 +54,17 @@ const char *fr_version(void);
  * ---------------------------------------------------------------------- */
 int fr_kb_lut(float kernel_width, float overgrid_factor, int length, float *lut_host);
 
+/* Exact LUT index from s = dk^2 without a square root (host computation).
+ * The reference index roundf(fl(fl(sqrtf(s)) / kHW) * (L-1)) (GridLut.cpp:
+ * 131-136) is a non-decreasing step function of s; thresholds[k] (k < L) is
+ * the smallest float s whose index is >= k (thresholds[0] = 0, +inf if never
+ * reached), thresholds[L] = +inf, *smax the smallest s with sqrtf(s) >= kHW
+ * (taps with s >= smax are outside the kernel), *kc = (L-1)/kHW.  The
+ * scatter kernel guesses k0 from an approximate square root, which lands on
+ * the exact index or one below, and corrects it with one comparison against
+ * thresholds[k0+1]. */
+int fr_lut_index_table(float kernel_width, int length, float *thresholds, float *smax, float *kc);
+
 /* ------------------------------------------------------------------------
  * Gridding plan: GridLut::plan + cuGridLut::plan
  * (ReconData/GridLut.h:20, GridLut.cpp:41-51, cuGridLut.cu:151-226)
@@ -163,6 +174,17 @@ int fr_fft_create(int dim, const unsigned *size, int batch, int sign, fr_fft *ou
 int fr_fft_execute(fr_fft fft, float *d_data, void *stream);
 int fr_fft_destroy(fr_fft fft);
 
+/* Backward FFT + fftShift + crop + SOS in one pruned pass
+ * (cuFFT.cpp:24-37, ImageFilter.cpp:40-53,159-209), for a grid flushed with
+ * FR_PLAN_CHECKERBOARD (even G, G = 2^a 3^b 5^c <= 1024): only the centred
+ * out_size crop is transformed through, and the last axis sums |x|^2 over the
+ * channels in channel order, takes the square root and divides by d_deapod
+ * (nullable, out_size floats).  d_out: out_size floats. */
+typedef struct fr_fftcs_s *fr_fftcs;
+int fr_fft_crop_sos_create(int dim, unsigned grid_size, int channels, const unsigned *out_size, fr_fftcs *out);
+int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deapod, float *d_out, void *stream);
+int fr_fft_crop_sos_destroy(fr_fftcs f);
+
 /* ImageFilter::fftShift (ImageFilter.cpp:40-53,231-280) on `channels`
  * images of `size`, in place, with the reference's swap semantics (also for
  * odd sizes). */
@@ -205,7 +227,9 @@ int fr_sos_map(const float *d_imgs, const float *d_maps, int channels, int dim, 
 typedef struct fr_recon_s *fr_recon;
 
 enum {
-    FR_RECON_DEAPODIZE = 1u << 0 /* divide by the kernel's image-domain apodization */
+    FR_RECON_DEAPODIZE = 1u << 0, /* divide by the kernel's image-domain apodization */
+    FR_RECON_CUFFT = 1u << 1      /* use the full cuFFT transform + SoS kernel even where the
+                                     pruned transform (fr_fft_crop_sos) applies */
 };
 
 typedef struct {

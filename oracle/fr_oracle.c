@@ -158,6 +158,14 @@ int orc_tap_lut_index(float dx, float dy, float dz, float kHW, int klength)
     return -1;
 }
 
+void orc_lut_index_of_s(const float *s, size_t n, float kHW, int klength, int *out)
+{
+    for (size_t i = 0; i < n; ++i) {
+        float dk = sqrtf(s[i]);
+        out[i] = dk < kHW ? (int)roundf(dk / kHW * (float)(klength - 1)) : -1;
+    }
+}
+
 /* GridLut::griddingChannel, GridLut.cpp:80-147. */
 void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, size_t n,
                       int dim, unsigned G, float kWidth, const float *lut, int klength,

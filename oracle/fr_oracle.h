@@ -57,6 +57,11 @@ void orc_sample_range(const float *traj, size_t n, int dim, unsigned G, float kH
  * the tap is outside the kernel radius. */
 int orc_tap_lut_index(float dx, float dy, float dz, float kHW, int klength);
 
+/* The same LUT index from s = dz^2 + dy^2 + dx^2 directly, for n values:
+ * out[i] = roundf(sqrtf(s[i]) / kHW * (klength - 1)) or -1 when
+ * sqrtf(s[i]) >= kHW (GridLut.cpp:131-136). */
+void orc_lut_index_of_s(const float *s, size_t n, float kHW, int klength, int *out);
+
 /* One channel of GridLut::griddingChannel (GridLut.cpp:80-147), FP32,
  * sequential in sample order.  out is G^d complex, overwritten. */
 void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, size_t n,

@@ -42,6 +42,7 @@ class Oracle:
                                            C.POINTER(C.c_float), C.POINTER(C.c_float)]
         lib.orc_sample_range.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _i32p, _i32p]
         lib.orc_tap_lut_index.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_int]
+        lib.orc_lut_index_of_s.argtypes = [_f32p, C.c_size_t, C.c_float, C.c_int, _i32p]
         lib.orc_grid_channel.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_uint,
                                          C.c_float, _f32p, C.c_int, _f32p]
         lib.orc_grid.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, C.c_int, C.c_int, C.c_uint,
@@ -105,6 +106,12 @@ class Oracle:
         out = np.zeros(n, np.float64)
         self.lib.orc_sample_mass(np.ascontiguousarray(traj_norm4, np.float32), n, dim, G, W,
                                  np.ascontiguousarray(lut, np.float32), len(lut), out, threads)
+        return out
+
+    def lut_index_of_s(self, s, kHW, L) -> np.ndarray:
+        s = np.ascontiguousarray(s, np.float32)
+        out = np.zeros(s.shape[0], np.int32)
+        self.lib.orc_lut_index_of_s(s, s.shape[0], kHW, L, out)
         return out
 
     def grid(self, traj_norm4, dcf, kdata, dim, G, W, lut, threads=1) -> np.ndarray:

@@ -82,3 +82,42 @@ def test_no_cpu_fallback_when_library_missing(tmp_path):
         assert "not built" in str(e)
     else:
         raise AssertionError("loading a missing library must raise")
+
+
+def lut_table(frlib, W, L):
+    thr = (C.c_float * (L + 1))()
+    smax, kc = C.c_float(), C.c_float()
+    assert frlib.fr_lut_index_table(W, L, thr, C.byref(smax), C.byref(kc)) == 0
+    return np.frombuffer(thr, np.float32).copy(), np.float32(smax.value), np.float32(kc.value)
+
+
+def device_lookup(s, thr, smax, kc, L, rel_err):
+    """The scatter kernel's index: approximate sqrt (relative error rel_err),
+    k0 = (int)fma(a, kc, 0.25) clamped to L-1, +1 when s >= thr[k0+1]."""
+    a = (np.sqrt(s.astype(np.float64)) * (1.0 + rel_err)).astype(np.float32)
+    g = (a.astype(np.float64) * np.float64(kc) + np.float64(np.float32(0.25))).astype(np.float32)
+    k0 = np.minimum(g.astype(np.int64), L - 1)
+    k = k0 + (s >= thr[k0 + 1]).astype(np.int64)
+    return np.where(s < smax, k, -1)
+
+
+def test_lut_index_table_is_exact(frlib, oracle):
+    """The square-root-free LUT index of the scatter kernel equals the
+    reference's roundf(sqrtf(s)/kHW*(L-1)) for every threshold, its float
+    neighbours, the kernel edge and random s, with the approximate square
+    root off by up to 2^-20 relative in either direction."""
+    rng = np.random.default_rng(0)
+    for W, L in [(4.0, 512), (4.0, 32), (5.0, 32), (3.0, 64), (6.0, 1024), (4.5, 512), (4.0, 4096)]:
+        thr, smax, kc = lut_table(frlib, W, L)
+        fin = thr[np.isfinite(thr)]
+        cand = [fin, np.nextafter(fin, np.float32(0)), np.nextafter(fin, np.float32(np.inf)),
+                np.array([0.0, smax, np.nextafter(smax, np.float32(0)), np.nextafter(smax, np.float32(np.inf))],
+                         np.float32),
+                rng.uniform(0, float(smax) * 1.05, 200000).astype(np.float32),
+                (rng.uniform(0, 1, 50000) ** 4 * float(smax)).astype(np.float32)]
+        s = np.abs(np.concatenate(cand)).astype(np.float32)
+        want = oracle.lut_index_of_s(s, W / 2, L)
+        for err in (-2.0 ** -20, 0.0, 2.0 ** -20):
+            got = device_lookup(s, thr, smax, kc, L, err)
+            bad = np.nonzero(got != want)[0]
+            assert bad.size == 0, (W, L, err, s[bad[:5]], got[bad[:5]], want[bad[:5]])
