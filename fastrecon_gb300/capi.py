@@ -61,6 +61,8 @@ _SIGS = {
     "fr_plan_profile_read": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "fr_kernel_launches": (C.c_longlong, []),
     "fr_grid": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "fr_grid_noalloc": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_uint, C.c_float, C.POINTER(C.c_float), C.c_int,
+                                  _VP, _VP, C.c_int, _VP, _VP]),
     "fr_fft_create": (C.c_int, [C.c_int, C.POINTER(C.c_uint), C.c_int, C.c_int, C.POINTER(_VP)]),
     "fr_fft_execute": (C.c_int, [_VP, _VP, _VP]),
     "fr_fft_destroy": (C.c_int, [_VP]),

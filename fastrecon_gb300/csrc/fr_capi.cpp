@@ -125,6 +125,34 @@ LutIndexTable lut_index_table(float hw, int L)
     return t;
 }
 
+void lut_index_table_into(float hw, int L, float *thr, float *smax, float *kc)
+{
+    unsigned lo = 0, hi = fbits(std::max(4.f * hw * hw, 1.f));
+    while (lo < hi) {
+        unsigned mid = lo + (hi - lo) / 2;
+        if (lut_reference_index(bitsf(mid), hw, L) < 0)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    const unsigned top = lo;
+    thr[0] = 0.f;
+    for (int k = 1; k <= L; ++k) thr[k] = INFINITY;
+    for (int k = 1; k < L; ++k) {
+        unsigned a = 0, b = top;
+        while (a < b) {
+            unsigned mid = a + (b - a) / 2;
+            if (lut_reference_index(bitsf(mid), hw, L) >= k)
+                b = mid;
+            else
+                a = mid + 1;
+        }
+        thr[k] = a < top ? bitsf(a) : INFINITY;
+    }
+    *smax = bitsf(top);
+    *kc = (float)(L - 1) / hw;
+}
+
 }  // namespace fr
 
 fr_plan_s::~fr_plan_s()

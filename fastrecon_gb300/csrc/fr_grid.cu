@@ -516,4 +516,83 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");
 }
 
+// --------------------------------------------------------------------------
+// The same scatter from a plan held in caller-provided memory
+// (fr_grid_noalloc): identical kernels and launch shapes, no allocation.
+// --------------------------------------------------------------------------
+namespace {
+template <int DIM, int R>
+int launch_into(const GridParams &P, long long nitems, long long nsplits, cudaStream_t s)
+{
+    size_t smem = grid_smem_bytes(P.K, R, P.L);
+    auto kern = grid_tiles_kernel<DIM, R>;
+    if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)nitems, (unsigned)P.ngroups);
+    kern<<<grid, kWarps * 32, smem, s>>>(P);
+    FR_CHECK_LAUNCH("grid_tiles_kernel");
+    if (nsplits > 0) {
+        dim3 g2((unsigned)nsplits, (unsigned)P.ngroups);
+        reduce_splits_kernel<R><<<g2, 256, 0, s>>>(P);
+        FR_CHECK_LAUNCH("reduce_splits_kernel");
+    }
+    return FR_OK;
+}
+}  // namespace
+
+size_t grid_partials_bytes(long long nslots, int channels, int coil_group, long long K)
+{
+    const long long ngroups = (channels + coil_group - 1) / coil_group;
+    return (size_t)nslots * ngroups * K * floats_per_cell(coil_group) * 4;
+}
+
+int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+              cudaStream_t s)
+{
+    const int R = floats_per_cell(gi.coil_group);
+    GridParams P;
+    P.traj = gi.traj;
+    P.recs = gi.recs;
+    P.items = gi.items;
+    P.splits = gi.splits;
+    P.kdata = d_kdata;
+    P.dcf = d_dcf;
+    P.lut_e = gi.lut_e;
+    P.grid = d_grid;
+    P.partials = gi.partials;
+    P.n = (long long)gi.n;
+    P.channels = channels;
+    P.coil_group = gi.coil_group;
+    P.ngroups = (channels + gi.coil_group - 1) / gi.coil_group;
+    P.dim = gi.dim;
+    P.G = (int)gi.G;
+    P.K = 1;
+    for (int d = 0; d < 3; ++d) {
+        P.tile[d] = gi.tile[d];
+        P.ntile[d] = gi.ntile[d];
+        P.K *= gi.tile[d];
+    }
+    P.L = gi.L;
+    P.smax = gi.smax;
+    P.kc = gi.kc;
+    P.khalf = 0.25f;
+    P.checkerboard = 0;
+    if (gi.nitems == 0) return FR_OK;
+    if (gi.dim == 3) {
+        switch (R) {
+        case 8: return launch_into<3, 8>(P, gi.nitems, gi.nsplits, s);
+        case 16: return launch_into<3, 16>(P, gi.nitems, gi.nsplits, s);
+        case 32: return launch_into<3, 32>(P, gi.nitems, gi.nsplits, s);
+        case 64: return launch_into<3, 64>(P, gi.nitems, gi.nsplits, s);
+        }
+    } else {
+        switch (R) {
+        case 8: return launch_into<2, 8>(P, gi.nitems, gi.nsplits, s);
+        case 16: return launch_into<2, 16>(P, gi.nitems, gi.nsplits, s);
+        case 32: return launch_into<2, 32>(P, gi.nitems, gi.nsplits, s);
+        case 64: return launch_into<2, 64>(P, gi.nitems, gi.nsplits, s);
+        }
+    }
+    return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");
+}
+
 }  // namespace fr

@@ -138,6 +138,58 @@ struct LutIndexTable {
 };
 int lut_reference_index(float s, float hw, int L);  // the reference formula on the host (-1 if invalid)
 LutIndexTable lut_index_table(float hw, int L);
+// The same table into caller storage: thr has L + 1 entries.
+void lut_index_table_into(float hw, int L, float *thr, float *smax, float *kc);
+
+// Plan into caller-provided device memory (no allocation).  The fixed-size
+// buffers are given; records, work items and split tiles are carved from
+// [rest, rest + rest_bytes) once their counts are known.
+struct PlanInto {
+    int dim;
+    unsigned G;
+    float hw;
+    int prefilter;
+    int tile[3], ntile[3];
+    long long ntiles;
+    int chunk;
+    int *bounds;  // 32 words
+    float4 *traj;
+    int *tile_count, *tile_fill;
+    TileScan *scan;         // ntiles + 1
+    TileScan *scan_blocks;  // plan_scan_blocks(ntiles)
+    unsigned char *rest;
+    size_t rest_bytes;
+};
+struct PlanIntoOut {
+    long long npairs, nitems, nslots, nsplits;
+    unsigned long long *recs;
+    WorkItem *items;
+    SplitTile *splits;
+    size_t rest_used;
+};
+long long plan_scan_blocks(long long ntiles);
+int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s, PlanIntoOut *out);
+
+// Grid from a plan held in caller-provided memory (no allocation).
+struct GridInto {
+    int dim;
+    unsigned G;
+    int tile[3], ntile[3];
+    int coil_group;
+    int L;
+    float smax, kc;
+    const float4 *traj;
+    const unsigned long long *recs;
+    const WorkItem *items;
+    const SplitTile *splits;
+    const float4 *lut_e;
+    long long nitems, nsplits;
+    size_t n;
+    float *partials;
+};
+size_t grid_partials_bytes(long long nslots, int channels, int coil_group, long long K);
+int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+              cudaStream_t s);
 }  // namespace fr
 
 namespace fr {

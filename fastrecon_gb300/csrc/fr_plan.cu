@@ -583,6 +583,77 @@ int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_o
     return FR_OK;
 }
 
+long long plan_scan_blocks(long long ntiles)
+{
+    return std::max<long long>((ntiles + kScanSeg - 1) / kScanSeg, 1);
+}
+
+// The plan of plan_run, into caller-provided buffers (fr_grid_noalloc).
+int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s, PlanIntoOut *out)
+{
+    const long long nblocks = (pi.ntiles + kScanSeg - 1) / kScanSeg;
+    int *b = pi.bounds;
+    FR_CUDA(cudaMemsetAsync(pi.tile_count, 0, pi.ntiles * 4, s));
+    FR_CUDA(cudaMemsetAsync(pi.tile_fill, 0, pi.ntiles * 4, s));
+    bounds_init_kernel<<<1, 32, 0, s>>>(b);
+    FR_CHECK_LAUNCH("bounds_init_kernel");
+    const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
+    if (n > 0) {
+        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, pi.dim, b);
+        FR_CHECK_LAUNCH("bounds_kernel");
+    }
+    scale_kernel<<<1, 1, 0, s>>>(b, pi.dim, pi.G);
+    FR_CHECK_LAUNCH("scale_kernel");
+    BinGeom g;
+    g.dim = pi.dim;
+    g.G = pi.G;
+    g.hw = pi.hw;
+    g.prefilter = pi.prefilter;
+    for (int d = 0; d < 3; ++d) {
+        g.tile[d] = pi.tile[d];
+        g.ntile[d] = pi.ntile[d];
+    }
+    if (n > 0) {
+        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, 0, pi.traj, pi.tile_count);
+        FR_CHECK_LAUNCH("normalize_count_kernel");
+    }
+    scan_reduce_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(pi.tile_count, pi.ntiles, pi.chunk, pi.scan_blocks);
+    FR_CHECK_LAUNCH("scan_reduce_kernel");
+    scan_blocks_kernel<<<1, kScanThreads, 0, s>>>(pi.scan_blocks, (int)nblocks);
+    FR_CHECK_LAUNCH("scan_blocks_kernel");
+    scan_write_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(pi.tile_count, pi.ntiles, pi.chunk, pi.scan_blocks,
+                                                            pi.scan);
+    FR_CHECK_LAUNCH("scan_write_kernel");
+    TileScan tot;
+    FR_CUDA(cudaMemcpyAsync(&tot, pi.scan + pi.ntiles, sizeof(TileScan), cudaMemcpyDeviceToHost, s));
+    FR_CUDA(cudaStreamSynchronize(s));
+    if (tot.pairs > 0xFFFFFFFFll || tot.items > INT_MAX || tot.slots > INT_MAX)
+        return fail(FR_ERR_UNSUPPORTED, "bin lists exceed 32-bit indexing");
+    // carve records, items and split tiles (256-byte aligned) from `rest`
+    auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t recs_b = align(std::max<long long>(tot.pairs, 1) * 8);
+    const size_t items_b = align(std::max<long long>(tot.items, 1) * sizeof(WorkItem));
+    const size_t splits_b = align(std::max<long long>(tot.splits, 1) * sizeof(SplitTile));
+    if (recs_b + items_b + splits_b > pi.rest_bytes)
+        return fail(FR_ERR_CAPACITY, "bin lists of this trajectory do not fit the no-allocation scratch");
+    out->npairs = tot.pairs;
+    out->nitems = tot.items;
+    out->nslots = tot.slots;
+    out->nsplits = tot.splits;
+    out->recs = reinterpret_cast<unsigned long long *>(pi.rest);
+    out->items = reinterpret_cast<WorkItem *>(pi.rest + recs_b);
+    out->splits = reinterpret_cast<SplitTile *>(pi.rest + recs_b + items_b);
+    out->rest_used = recs_b + items_b + splits_b;
+    if (n > 0) {
+        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(pi.traj, n, g, pi.scan, pi.tile_fill, out->recs);
+        FR_CHECK_LAUNCH("fill_kernel");
+    }
+    items_kernel<<<grid_blocks(pi.ntiles, 256), 256, 0, s>>>(pi.tile_count, pi.scan, pi.ntiles, pi.chunk, out->items,
+                                                             out->splits);
+    FR_CHECK_LAUNCH("items_kernel");
+    return FR_OK;
+}
+
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s)
 {
     if (p->n == 0) return FR_OK;

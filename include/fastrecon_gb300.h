@@ -164,6 +164,31 @@ int fr_grid(fr_plan plan, const float *d_kdata, const float *d_dcf, int channels
             float *d_grid, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Gridding without device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot let a library allocate device memory during their
+ * work -- a scanner's real-time reconstruction loop that reserves its memory
+ * at start-up, or a host framework whose caching allocator already holds the
+ * device memory.  Does what fr_plan_create (default tiling) +
+ * fr_plan_set_trajectory + fr_grid do, with every plan and scatter buffer
+ * taken from one fixed scratch array of FR_NOALLOC_SCRATCH_BYTES (32 MiB)
+ * in device memory that each GPU loading the library holds until exit; it
+ * calls no cudaMalloc or cudaFree.  Enough for a 2D radial trajectory of
+ * 512 x 1024 samples (0.5 M) on a 512^2 grid; 1024 x 1024 is already too
+ * large.  Larger trajectories, tile tables or split-tile partials are
+ * rejected with FR_ERR_CAPACITY before any GPU work on them.
+ * lut_length <= FR_NOALLOC_MAX_LUT.  The first call on a device looks the
+ * scratch up (make it before any stream capture).  All calls share the
+ * scratch: calls that overlap on the GPU (other streams or host threads) race.
+ * Synchronises `stream` once.  Same arguments and output as fr_grid.
+ * ---------------------------------------------------------------------- */
+#define FR_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define FR_NOALLOC_MAX_LUT 1024
+int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned grid_size, float kernel_width,
+                    const float *lut_host, int lut_length, const float *d_kdata, const float *d_dcf, int channels,
+                    float *d_grid, void *stream);
+
+/* ------------------------------------------------------------------------
  * FFT stage: cuFFT::plan / cuFFT::excute (ImageFilter/cuFFT.cpp:15-37),
  * ImageFilter::fftPlan / fftExecute (ImageFilter.cpp:211-229).
  * In-place unnormalised C2C transform of `batch` contiguous images;
