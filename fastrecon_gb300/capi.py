@@ -63,6 +63,28 @@ _SIGS = {
     "fr_grid": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
     "fr_grid_noalloc": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_uint, C.c_float, C.POINTER(C.c_float), C.c_int,
                                   _VP, _VP, C.c_int, _VP, _VP]),
+    "fr_batch_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(_VP)]),
+    "fr_batch_destroy": (C.c_int, [_VP]),
+    "fr_batch_set_trajectories": (C.c_int, [_VP, _VP, C.POINTER(C.c_size_t), C.c_int, _VP]),
+    "fr_batch_stats": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
+    "fr_batch_grid": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "fr_batch_capture": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "fr_batch_replay": (C.c_int, [_VP, _VP]),
+    "fr_batch_autotune": (C.c_int, [C.POINTER(PlanDesc), _VP, C.POINTER(C.c_size_t), C.c_int, _VP, _VP, C.c_int, _VP,
+                                    C.c_int, C.POINTER(PlanDesc), C.POINTER(C.c_float), _VP]),
+    "fr_dcf_analytic": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_float, _VP, _VP]),
+    "fr_degrid": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),
+    "fr_grid_real": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "fr_dcf_pipe": (C.c_int, [_VP, C.c_int, _VP, _VP]),
+    "fr_density_counts": (C.c_int, [_VP, C.POINTER(C.c_int), C.c_int, _VP, _VP]),
+    "fr_dcf_features": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_int), C.c_int, C.c_float, _VP, _VP]),
+    "fr_mlp_forward": (C.c_int, [_VP, _VP, C.c_size_t, C.c_uint, _VP, _VP]),
+    "fr_mlp_workspace_bytes": (C.c_size_t, [C.c_size_t]),
+    "fr_mlp_backward": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP, _VP, _VP]),
+    "fr_mlp_adam": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                              _VP]),
+    "fr_mlp_to_bf16": (C.c_int, [_VP, _VP, C.c_int, _VP]),
     "fr_fft_create": (C.c_int, [C.c_int, C.POINTER(C.c_uint), C.c_int, C.c_int, C.POINTER(_VP)]),
     "fr_fft_execute": (C.c_int, [_VP, _VP, _VP]),
     "fr_fft_destroy": (C.c_int, [_VP]),

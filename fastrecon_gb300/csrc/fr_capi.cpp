@@ -405,6 +405,91 @@ int fr_grid(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, f
 }
 
 // --------------------------------------------------------------------------
+// Density compensation and degridding
+// --------------------------------------------------------------------------
+
+int fr_dcf_analytic(const float *d_traj, size_t n, int dim, float power, float *d_dcf, void *stream)
+{
+    if (dim < 1 || dim > 3) return fail(FR_ERR_INVALID_ARGUMENT, "dim must be 1, 2 or 3");
+    if (n && (!d_traj || !d_dcf)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_traj) & 15) return fail(FR_ERR_INVALID_ARGUMENT, "trajectory must be 16-byte aligned");
+    if (!(power >= 0.f)) return fail(FR_ERR_INVALID_ARGUMENT, "power must be >= 0");
+    return dcf_analytic_run(d_traj, n, dim, power, d_dcf, (cudaStream_t)stream);
+}
+
+int fr_degrid(fr_plan p, const float *d_grid, int channels, float *d_kdata, void *stream)
+{
+    if (!p || (p->n && (!d_grid || !d_kdata))) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_grid) & 7) || (reinterpret_cast<uintptr_t>(d_kdata) & 7))
+        return fail(FR_ERR_INVALID_ARGUMENT, "complex buffers must be 8-byte aligned");
+    return degrid_run(p, d_grid, channels, d_kdata, (cudaStream_t)stream);
+}
+
+int fr_grid_real(fr_plan p, const float *d_w, float *d_grid, void *stream)
+{
+    if (!p || !d_grid || (p->n && !d_w)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return grid_real_run(p, d_w, d_grid, (cudaStream_t)stream);
+}
+
+int fr_dcf_pipe(fr_plan p, int iterations, float *d_dcf, void *stream)
+{
+    if (!p || (p->n && !d_dcf)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return dcf_pipe_run(p, iterations, d_dcf, (cudaStream_t)stream);
+}
+
+// --------------------------------------------------------------------------
+// Learned DCF: density features and the network
+// --------------------------------------------------------------------------
+
+int fr_density_counts(fr_plan p, const int *radii, int nradii, int *d_counts, void *stream)
+{
+    if (!p || (p->n && !d_counts)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return density_counts_run(p, radii, nradii, d_counts, (cudaStream_t)stream);
+}
+
+int fr_dcf_features(fr_plan p, const int *d_counts, const float *d_raw_traj, const int *radii, int nradii, float kmax,
+                    float *d_features, void *stream)
+{
+    if (!p || (p->n && (!d_counts || !d_raw_traj || !d_features))) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_raw_traj) & 15) return fail(FR_ERR_INVALID_ARGUMENT, "trajectory must be 16-byte aligned");
+    if (p->small.reserve(256)) return FR_ERR_CUDA;
+    return dcf_features_run(d_counts, d_raw_traj, p->n, p->dim, radii, nradii, kmax, d_features,
+                            p->small.as<unsigned>(), (cudaStream_t)stream);
+}
+
+int fr_mlp_forward(const void *d_params, const float *d_features, size_t n, unsigned flags, float *d_out, void *stream)
+{
+    if (n && (!d_params || !d_features || !d_out)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_params) & 1) return fail(FR_ERR_INVALID_ARGUMENT, "parameters must be 2-byte aligned");
+    return mlp_forward_run(d_params, d_features, n, (flags & FR_MLP_EXP) ? 1 : 0, d_out, (cudaStream_t)stream);
+}
+
+size_t fr_mlp_workspace_bytes(size_t n) { return mlp_workspace_bytes(n); }
+
+int fr_mlp_backward(const void *d_params, const float *d_features, const float *d_target, const float *d_weight,
+                    size_t n, void *d_workspace, float *d_grad, float *d_loss, void *stream)
+{
+    if (!d_params || !d_features || !d_target || !d_workspace || !d_grad)
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_workspace) & 15) return fail(FR_ERR_INVALID_ARGUMENT, "workspace must be 16-byte aligned");
+    return mlp_backward_run(d_params, d_features, d_target, d_weight, n, d_workspace, d_grad, d_loss,
+                            (cudaStream_t)stream);
+}
+
+int fr_mlp_adam(float *d_master, void *d_params, const float *d_grad, float *d_m, float *d_v, int count, float lr,
+                float beta1, float beta2, float eps, int step, void *stream)
+{
+    if (!d_master || !d_params || !d_grad || !d_m || !d_v) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return mlp_adam_run(d_master, d_params, d_grad, d_m, d_v, count, lr, beta1, beta2, eps, step, (cudaStream_t)stream);
+}
+
+int fr_mlp_to_bf16(const float *d_master, void *d_params, int count, void *stream)
+{
+    if (count > 0 && (!d_master || !d_params)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return to_bf16_run(d_master, d_params, count, (cudaStream_t)stream);
+}
+
+// --------------------------------------------------------------------------
 // cuFFT stage
 // --------------------------------------------------------------------------
 

@@ -43,6 +43,14 @@ struct GridParams {
     int L;
     float smax, kc, khalf;  // exact LUT index from s = dk^2 (LutIndexTable)
     int checkerboard;
+    // batches of frames (nullptr / 0 for one trajectory): frame f owns
+    // samples [frame_off[f], frame_off[f+1]), its k-space block starts at
+    // channels * frame_off[f] complex values, its grid at f * grid_frame_floats;
+    // work items and split tiles carry their frame in `pad`.
+    const long long *frame_off;
+    long long grid_frame_floats;
+    int *work_counter;  // persistent kernel: next work index
+    long long nwork;    // persistent kernel: nitems * ngroups
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -113,8 +121,8 @@ __device__ __forceinline__ unsigned lds_u8(unsigned a)
 // (x pair, row): each writes two consecutive x cells as one 16-byte store
 // (even tile x extent and grid size), rows advance without divisions.
 template <int R>
-__device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned acc, int cg, int ox, int oy, int oz,
-                                                 bool zero)
+__device__ __forceinline__ void write_cell_group(const GridParams &P, float *gridf, unsigned acc, int cg, int ox, int oy,
+                                                 int oz, bool zero)
 {
     const int CG = P.coil_group;
     const int Tx = P.tile[0], Ty = P.tile[1], Tz = P.tile[2];
@@ -124,7 +132,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned a
     const size_t cells = P.dim == 3 ? G * G * G : G * G;
     const int rows = Ty * Tz;
     const bool pairs = (Tx % 2 == 0) && (P.G % 2 == 0) && ((int)blockDim.x % (Tx / 2) == 0) &&
-                       ((reinterpret_cast<uintptr_t>(P.grid) & 15) == 0);
+                       ((reinterpret_cast<uintptr_t>(gridf) & 15) == 0);
     if (pairs) {
         const int hx = Tx / 2;
         const int lx = 2 * (threadIdx.x % hx), rr0 = threadIdx.x / hx, rstep = blockDim.x / hx;
@@ -132,7 +140,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned a
         const int gx = ox + lx;
         const bool xin = gx < P.G;  // gx even, G even: gx + 1 < G as well
         for (int cl = 0; cl < ncl; ++cl) {
-            float4 *gridc = reinterpret_cast<float4 *>(P.grid + 2 * (size_t)(cg * CG + cl) * cells);
+            float4 *gridc = reinterpret_cast<float4 *>(gridf + 2 * (size_t)(cg * CG + cl) * cells);
             int ly = rr0 % Ty, lz = rr0 / Ty;
             for (int r = rr0; r < rows; r += rstep) {
                 const int gy = oy + ly, gz = oz + lz;
@@ -166,7 +174,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned a
         return;
     }
     const int K = P.K;
-    float2 *grid = reinterpret_cast<float2 *>(P.grid);
+    float2 *grid = reinterpret_cast<float2 *>(gridf);
     for (int idx = threadIdx.x; idx < ncl * K; idx += blockDim.x) {
         int cl = idx / K;
         int i = idx - cl * K;
@@ -191,41 +199,54 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, unsigned a
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
 
-template <int DIM, int R>
-__global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
+// Shared-memory layout of the scatter: accumulator tile [K][R] floats | LUT
+// entries [L] float4 | per warp two tap-list buffers [32] {byte offset of the
+// tap's cell row (swizzled), weight} | tap decode table [16][64] bytes.
+template <int R>
+__device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
 {
-    extern __shared__ float4 smem4[];
-    const int K = P.K;
-    // shared layout: accumulator tile [K][R] floats | LUT entries [L] float4 |
-    // per warp two tap-list buffers [32] {byte offset of the tap's cell row
-    // (swizzled), weight} | tap decode table [16][64] bytes
-    const unsigned acc = smem_addr(smem4);
-    const unsigned lutE = acc + (unsigned)K * R * 4u;
-    const unsigned lists = lutE + (unsigned)P.L * 16u;
-    const unsigned dec = lists + (unsigned)(kWarps * 2 * kListEntries * 8);
-    float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)K * R);
+    float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)P.K * R);
     unsigned char *dec_g = reinterpret_cast<unsigned char *>(lutE_g + P.L) + kWarps * 2 * kListEntries * 8;
-
-    const WorkItem it = P.items[blockIdx.x];
-    const int cg = blockIdx.y;
-    const int t = it.tile;
-    const int tx = t % P.ntile[0];
-    const int ty = (t / P.ntile[0]) % P.ntile[1];
-    const int tz = t / (P.ntile[0] * P.ntile[1]);
-    const int ox = tx * P.tile[0], oy = ty * P.tile[1], oz = tz * P.tile[2];
-
-    if (it.count == 0) {  // empty tile: stream zeros
-        write_cell_group<R>(P, acc, cg, ox, oy, oz, true);
-        return;
-    }
-
-    for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutE_g[i] = P.lut_e[i];
     for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
         const int nx = (i >> 8) + 1, ny = ((i >> 6) & 3) + 1, tt = i & 63;
         const int ix = tt % nx, iy = (tt / nx) % ny, iz = tt / (nx * ny);
         dec_g[i] = (unsigned char)(ix | (iy << 2) | ((iz & 3) << 4));
     }
+}
+
+// One work item for one coil group: zero the tile, accumulate the item's
+// samples, flush (or write the partial tile).  The LUT and decode tables must
+// be staged; the caller synchronises the CTA before the next item.
+template <int DIM, int R>
+__device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &it, int cg, float4 *smem4)
+{
+    const int K = P.K;
+    const unsigned acc = smem_addr(smem4);
+    const unsigned lutE = acc + (unsigned)K * R * 4u;
+    const unsigned lists = lutE + (unsigned)P.L * 16u;
+    const unsigned dec = lists + (unsigned)(kWarps * 2 * kListEntries * 8);
+
+    const int t = it.tile;
+    const int tx = t % P.ntile[0];
+    const int ty = (t / P.ntile[0]) % P.ntile[1];
+    const int tz = t / (P.ntile[0] * P.ntile[1]);
+    const int ox = tx * P.tile[0], oy = ty * P.tile[1], oz = tz * P.tile[2];
+
+    // frame of this item (a single trajectory is frame 0 of one)
+    const int f = P.frame_off ? it.pad : 0;
+    const long long s_off = P.frame_off ? P.frame_off[f] : 0;
+    const long long n_f = P.frame_off ? P.frame_off[f + 1] - s_off : P.n;
+    float *gridf = P.grid + (size_t)f * (size_t)P.grid_frame_floats;
+    const float4 *traj = P.traj + s_off;
+    const float *dcf = P.dcf + s_off;
+
+    if (it.count == 0) {  // empty tile: stream zeros
+        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, true);
+        return;
+    }
+
+    for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -245,11 +266,12 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
     bool coil_ok[NF];
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-        const int f = f0 + 32 * k;
-        const int coil = cg * CG + (f >> 1);
-        coil_ok[k] = (f >> 1) < CG && coil < P.channels;
+        const int fl = f0 + 32 * k;
+        const int coil = cg * CG + (fl >> 1);
+        coil_ok[k] = (fl >> 1) < CG && coil < P.channels;
         // real or imaginary float of this coil's sample s is kdf[k][2 * s]
-        kdf[k] = P.kdata + 2 * (size_t)(coil_ok[k] ? coil : 0) * (size_t)P.n + (f & 1);
+        kdf[k] = P.kdata + 2 * (size_t)P.channels * (size_t)s_off +
+                 2 * (size_t)(coil_ok[k] ? coil : 0) * (size_t)n_f + (fl & 1);
     }
     const unsigned long long *recs = P.recs + it.begin;
 
@@ -263,8 +285,8 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
         const int nx = (box >> 18) & 15, ny = (box >> 22) & 15, nz = (box >> 26) & 15;
         const int ntap = nx * ny * nz;
         if (ntap == 0) continue;
-        const float4 p = P.traj[s];
-        const float d = P.dcf[s];
+        const float4 p = traj[s];
+        const float d = dcf[s];
         float val[NF];
 #pragma unroll
         for (int k = 0; k < NF; ++k)
@@ -347,11 +369,47 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
     __syncthreads();
 
     if (it.slot < 0) {
-        write_cell_group<R>(P, acc, cg, ox, oy, oz, false);
+        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, false);
     } else {
         float4 *dst = reinterpret_cast<float4 *>(
             P.partials + ((size_t)it.slot * P.ngroups + cg) * (size_t)K * R);
         for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) dst[i] = smem4[i];
+    }
+}
+
+// One CTA per (work item, coil group).
+template <int DIM, int R>
+__global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
+{
+    extern __shared__ float4 smem4[];
+    const WorkItem it = P.items[blockIdx.x];
+    if (it.count > 0) {
+        stage_tables<R>(P, smem4);
+        // grid_item's first barrier (after zeroing the tile) orders the staging
+    }
+    grid_item<DIM, R>(P, it, blockIdx.y, smem4);
+}
+
+// Persistent: as many CTAs as fit on the GPU, each taking work indices
+// (coil group major, then item) from a counter until none are left.  Used
+// for batches of frames with uneven sample counts; the counter is zeroed
+// before each launch.
+template <int DIM, int R>
+__global__ void __launch_bounds__(512) grid_persistent_kernel(GridParams P)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ long long next;
+    stage_tables<R>(P, smem4);
+    const long long nitems = P.nwork / P.ngroups;
+    for (;;) {
+        __syncthreads();  // the previous item's flush is done with the tile
+        if (threadIdx.x == 0) next = atomicAdd(P.work_counter, 1);
+        __syncthreads();
+        const long long w = next;
+        if (w >= P.nwork) break;
+        const int cg = (int)(w / nitems);
+        const WorkItem it = P.items[w - (long long)cg * nitems];
+        grid_item<DIM, R>(P, it, cg, smem4);
     }
 }
 
@@ -368,7 +426,7 @@ __global__ void reduce_splits_kernel(GridParams P)
     const int K = P.K, CG = P.coil_group;
     const size_t G = (size_t)P.G;
     const size_t cells = P.dim == 3 ? G * G * G : G * G;
-    float2 *grid = reinterpret_cast<float2 *>(P.grid);
+    float2 *grid = reinterpret_cast<float2 *>(P.grid + (P.frame_off ? (size_t)st.pad * (size_t)P.grid_frame_floats : 0));
     const size_t slot_stride = (size_t)P.ngroups * K * R;
     const float *base = P.partials + ((size_t)st.first_slot * P.ngroups + cg) * (size_t)K * R;
     const int total = CG * K;
@@ -492,6 +550,10 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.kc = p->lut_kc;
     P.khalf = 0.25f;  // 0.5 - slack 0.25: the guess is the exact index or one below
     P.checkerboard = (p->flags & FR_PLAN_CHECKERBOARD) ? 1 : 0;
+    P.frame_off = nullptr;
+    P.grid_frame_floats = 0;
+    P.work_counter = nullptr;
+    P.nwork = 0;
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;
         if (p->partials.reserve(bytes)) return FR_ERR_OUT_OF_MEMORY;
@@ -576,6 +638,10 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.kc = gi.kc;
     P.khalf = 0.25f;
     P.checkerboard = 0;
+    P.frame_off = nullptr;
+    P.grid_frame_floats = 0;
+    P.work_counter = nullptr;
+    P.nwork = 0;
     if (gi.nitems == 0) return FR_OK;
     if (gi.dim == 3) {
         switch (R) {
@@ -590,6 +656,118 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
         case 16: return launch_into<2, 16>(P, gi.nitems, gi.nsplits, s);
         case 32: return launch_into<2, 32>(P, gi.nitems, gi.nsplits, s);
         case 64: return launch_into<2, 64>(P, gi.nitems, gi.nsplits, s);
+        }
+    }
+    return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");
+}
+
+// --------------------------------------------------------------------------
+// Batches of frames: one persistent launch over every frame's work items.
+// --------------------------------------------------------------------------
+namespace {
+template <int DIM, int R>
+int batch_setup_t(long long K, int L, int *blocks)
+{
+    const size_t smem = grid_smem_bytes(K, R, L);
+    auto kern = grid_persistent_kernel<DIM, R>;
+    if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0, dev = 0, sms = 0;
+    FR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem));
+    FR_CUDA(cudaGetDevice(&dev));
+    FR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (per_sm < 1) return fail(FR_ERR_UNSUPPORTED, "persistent scatter does not fit on an SM");
+    *blocks = per_sm * sms;
+    return FR_OK;
+}
+
+template <int DIM, int R>
+int batch_launch_t(const GridParams &P, int blocks, long long nsplits, cudaStream_t s)
+{
+    const size_t smem = grid_smem_bytes(P.K, R, P.L);
+    FR_CUDA(cudaMemsetAsync(P.work_counter, 0, sizeof(int), s));
+    const long long nb = std::min<long long>(blocks, P.nwork);
+    grid_persistent_kernel<DIM, R><<<(unsigned)nb, kWarps * 32, smem, s>>>(P);
+    FR_CHECK_LAUNCH("grid_persistent_kernel");
+    if (nsplits > 0) {
+        dim3 g2((unsigned)nsplits, (unsigned)P.ngroups);
+        reduce_splits_kernel<R><<<g2, 256, 0, s>>>(P);
+        FR_CHECK_LAUNCH("reduce_splits_kernel");
+    }
+    return FR_OK;
+}
+}  // namespace
+
+int batch_grid_setup(int dim, long long K, int coil_group, int L, int *blocks)
+{
+    const int R = floats_per_cell(coil_group);
+    if (grid_smem_bytes(K, R, L) > 227 * 1024) return fail(FR_ERR_UNSUPPORTED, "tile does not fit in shared memory");
+#define FR_BATCH_SETUP(D)                                                   \
+    switch (R) {                                                            \
+    case 8: return batch_setup_t<D, 8>(K, L, blocks);                       \
+    case 16: return batch_setup_t<D, 16>(K, L, blocks);                     \
+    case 32: return batch_setup_t<D, 32>(K, L, blocks);                     \
+    case 64: return batch_setup_t<D, 64>(K, L, blocks);                     \
+    }
+    if (dim == 3) {
+        FR_BATCH_SETUP(3)
+    } else {
+        FR_BATCH_SETUP(2)
+    }
+#undef FR_BATCH_SETUP
+    return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");
+}
+
+int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+                   cudaStream_t s)
+{
+    const int R = floats_per_cell(b.coil_group);
+    GridParams P;
+    P.traj = b.traj;
+    P.recs = b.recs;
+    P.items = b.items;
+    P.splits = b.splits;
+    P.kdata = d_kdata;
+    P.dcf = d_dcf;
+    P.lut_e = b.lut_e;
+    P.grid = d_grid;
+    P.partials = b.partials;
+    P.n = b.n_total;
+    P.channels = channels;
+    P.coil_group = b.coil_group;
+    P.ngroups = (channels + b.coil_group - 1) / b.coil_group;
+    P.dim = b.dim;
+    P.G = (int)b.G;
+    P.K = 1;
+    for (int d = 0; d < 3; ++d) {
+        P.tile[d] = b.tile[d];
+        P.ntile[d] = b.ntile[d];
+        P.K *= b.tile[d];
+    }
+    P.L = b.L;
+    P.smax = b.smax;
+    P.kc = b.kc;
+    P.khalf = 0.25f;
+    P.checkerboard = b.checkerboard;
+    P.frame_off = b.frame_off;
+    const size_t cells = b.dim == 3 ? (size_t)b.G * b.G * b.G : (size_t)b.G * b.G;
+    P.grid_frame_floats = (long long)(2 * (size_t)channels * cells);
+    P.work_counter = b.work_counter;
+    P.nwork = b.nitems * P.ngroups;
+    if (P.nwork == 0) return FR_OK;
+    if (P.nwork > 0x7FFFFFFFll) return fail(FR_ERR_UNSUPPORTED, "too many work items");
+    if (b.dim == 3) {
+        switch (R) {
+        case 8: return batch_launch_t<3, 8>(P, b.blocks, b.nsplits, s);
+        case 16: return batch_launch_t<3, 16>(P, b.blocks, b.nsplits, s);
+        case 32: return batch_launch_t<3, 32>(P, b.blocks, b.nsplits, s);
+        case 64: return batch_launch_t<3, 64>(P, b.blocks, b.nsplits, s);
+        }
+    } else {
+        switch (R) {
+        case 8: return batch_launch_t<2, 8>(P, b.blocks, b.nsplits, s);
+        case 16: return batch_launch_t<2, 16>(P, b.blocks, b.nsplits, s);
+        case 32: return batch_launch_t<2, 32>(P, b.blocks, b.nsplits, s);
+        case 64: return batch_launch_t<2, 64>(P, b.blocks, b.nsplits, s);
         }
     }
     return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");

@@ -99,6 +99,10 @@ struct fr_plan_s {
     fr::DevBuf splits;        // nsplits SplitTile
     fr::DevBuf partials;      // nslots * ngroups * K * R floats
     fr::DevBuf ranges;        // scratch for fr_plan_sample_ranges (unused otherwise)
+    fr::DevBuf real_grid;     // G^d floats: Pipe-Menon weight grid
+    fr::DevBuf real_partials; // nslots * K floats: split tiles of the real-valued scatter
+    fr::DevBuf density_sat;   // G^d ints: per-cell counts -> summed-area table
+    fr::DevBuf small;         // 256 bytes of scratch (feature max |k|)
 
     // scatter-kernel timing (fr_plan_profile)
     bool profile = false;
@@ -188,8 +192,53 @@ struct GridInto {
     float *partials;
 };
 size_t grid_partials_bytes(long long nslots, int channels, int coil_group, long long K);
+
+// Gridding of a batch of frames in one persistent launch (fr_batch_*).
+struct BatchGrid {
+    int dim;
+    unsigned G;
+    int tile[3], ntile[3];
+    int coil_group;
+    int L;
+    float smax, kc;
+    int checkerboard;
+    const float4 *traj;               // all frames, normalised, concatenated
+    const unsigned long long *recs;   // all frames' bin records (frame-local sample index)
+    const WorkItem *items;            // pad = frame
+    const SplitTile *splits;          // pad = frame
+    const float4 *lut_e;
+    const long long *frame_off;       // frames + 1 sample offsets (device)
+    long long nitems, nsplits, n_total;
+    float *partials;
+    int *work_counter;
+    int blocks;                       // persistent CTAs (batch_grid_setup)
+};
+// Sets the kernel attributes for a configuration and returns how many
+// persistent CTAs fill the GPU.  Call outside stream capture.
+int batch_grid_setup(int dim, long long K, int coil_group, int L, int *blocks);
+int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+                   cudaStream_t s);
 int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
               cudaStream_t s);
+}  // namespace fr
+
+namespace fr {
+// Density compensation and degridding (fr_dcf.cu).
+int dcf_analytic_run(const float *d_traj, size_t n, int dim, float power, float *d_out, cudaStream_t s);
+int degrid_run(fr_plan p, const float *d_grid, int channels, float *d_out, cudaStream_t s);
+int grid_real_run(fr_plan p, const float *d_w, float *d_grid, cudaStream_t s);
+int dcf_pipe_run(fr_plan p, int iterations, float *d_w, cudaStream_t s);
+// Density features (fr_density.cu) and the DCF network (fr_mlp.cu).
+int density_counts_run(fr_plan p, const int *radii, int nradii, int *d_counts, cudaStream_t s);
+int dcf_features_run(const int *d_counts, const float *d_raw, size_t n, int dim, const int *radii, int nradii,
+                     float kmax, float *d_feat, unsigned *d_scratch, cudaStream_t s);
+size_t mlp_workspace_bytes(size_t n);
+int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, float *d_y, cudaStream_t s);
+int mlp_backward_run(const void *d_params, const float *d_x, const float *d_t, const float *d_w, size_t n, void *ws,
+                     float *d_grad, float *d_loss, cudaStream_t s);
+int mlp_adam_run(float *d_master, void *d_params, const float *d_grad, float *d_m, float *d_v, int count, float lr,
+                 float beta1, float beta2, float eps, int step, cudaStream_t s);
+int to_bf16_run(const float *d_a, void *d_b, int count, cudaStream_t s);
 }  // namespace fr
 
 namespace fr {

@@ -154,6 +154,44 @@ class GridPlan:
               "fr_grid")
         return out
 
+    def degrid(self, grid, out=None, stream=None):
+        """grid: (C, G^d) complex64 CUDA -> (C, N) complex64 samples (adjoint of ``grid`` without DCF)."""
+        torch = _torch()
+        assert grid.dtype == torch.complex64 and grid.is_cuda
+        grid = grid.contiguous().reshape(-1, self.cells)
+        ch = grid.shape[0]
+        if out is None:
+            out = torch.empty((ch, self.n), dtype=torch.complex64, device="cuda")
+        check(self.lib.fr_degrid(self.h, _ptr(grid), ch, _ptr(out), C.c_void_p(_stream(stream))), "fr_degrid")
+        return out
+
+    def grid_real(self, w, out=None, stream=None):
+        """Real-valued gridding of per-sample weights: (N,) float32 -> (G^d,) float32."""
+        torch = _torch()
+        w = w.contiguous()
+        if out is None:
+            out = torch.empty(self.cells, dtype=torch.float32, device="cuda")
+        check(self.lib.fr_grid_real(self.h, _ptr(w), _ptr(out), C.c_void_p(_stream(stream))), "fr_grid_real")
+        return out
+
+    def dcf_pipe(self, iterations: int = 20, w0=None, stream=None):
+        """Pipe-Menon iterative DCF on this plan's trajectory and kernel."""
+        torch = _torch()
+        w = torch.ones(self.n, dtype=torch.float32, device="cuda") if w0 is None else w0.clone().contiguous()
+        check(self.lib.fr_dcf_pipe(self.h, int(iterations), _ptr(w), C.c_void_p(_stream(stream))), "fr_dcf_pipe")
+        return w
+
+
+def dcf_analytic(traj, dim: int, power: float = 1.0, stream=None):
+    """|k|^power of raw (un-normalised) Point<float> coordinates on the device."""
+    torch = _torch()
+    assert traj.is_cuda and traj.dtype == torch.float32 and traj.shape[-1] == 4
+    traj = traj.contiguous()
+    out = torch.empty(traj.shape[0], dtype=torch.float32, device="cuda")
+    check(capi.load().fr_dcf_analytic(_ptr(traj), traj.shape[0], dim, float(power), _ptr(out),
+                                      C.c_void_p(_stream(stream))), "fr_dcf_analytic")
+    return out
+
 
 class FFT:
     """cuFFT::plan / excute: in-place unnormalised C2C over a batch of images."""

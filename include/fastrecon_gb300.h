@@ -189,6 +189,99 @@ int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned grid_size, 
                     float *d_grid, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Batches: many frames (time frames of a dynamic scan, or volumes) with
+ * uneven sample counts gridded in ONE persistent launch, replayable as a
+ * captured CUDA graph.  No counterpart in the reference, which grids one
+ * dataset per GridLut::execute (GridLut.cpp:53-78).
+ *
+ * Frame f owns samples [offsets[f], offsets[f+1]) of the concatenated raw
+ * trajectory and is normalised with its own bounds (ReconData.cpp:201-225).
+ * k-space: frame-major, frame f is a channels x n_f complex64 block at
+ * complex offset channels * offsets[f]; DCF concatenated like the samples;
+ * grid: frames x channels x G^d complex64.
+ * ---------------------------------------------------------------------- */
+typedef struct fr_batch_s *fr_batch;
+int fr_batch_create(const fr_plan_desc *desc, fr_batch *out);
+int fr_batch_destroy(fr_batch batch);
+/* Plans every frame (synchronises `stream`); offsets has frames + 1 entries. */
+int fr_batch_set_trajectories(fr_batch batch, const float *d_traj, const size_t *offsets, int frames, void *stream);
+int fr_batch_stats(fr_batch batch, long long *frames, long long *samples, long long *items, long long *slots,
+                   int *persistent_ctas);
+int fr_batch_grid(fr_batch batch, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+                  void *stream);
+/* Capture fr_batch_grid on `stream` (a created stream, not the legacy
+ * default stream) into a CUDA graph bound to these buffers; fr_batch_replay
+ * launches it (the buffers' contents are read at replay time). */
+int fr_batch_capture(fr_batch batch, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
+                     void *stream);
+int fr_batch_replay(fr_batch batch, void *stream);
+/* Times fr_batch_grid over tile shapes, bin chunks and coil groups on the
+ * given data and returns the fastest descriptor (base supplies the rest). */
+int fr_batch_autotune(const fr_plan_desc *base, const float *d_traj, const size_t *offsets, int frames,
+                      const float *d_kdata, const float *d_dcf, int channels, float *d_grid, int repeats,
+                      fr_plan_desc *best, float *best_ms, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Density compensation and degridding.  No counterpart in the reference,
+ * which reads its DCF from a file (ReconData.cpp:108-121).
+ * ---------------------------------------------------------------------- */
+/* |k|^power of the RAW coordinates (Point<float> per sample, before
+ * normalisation): |k| = sqrt(x^2 + y^2 [+ z^2]) in double; power 1 -> |k|
+ * (2D radial ramp), power 2 -> |k|*|k| (3D radial), else pow(|k|, power). */
+int fr_dcf_analytic(const float *d_traj, size_t n, int dim, float power, float *d_dcf, void *stream);
+/* Interpolate a channels x G^d complex grid at the plan's samples into
+ * channels x n complex64 (the adjoint of fr_grid without DCF: same cell
+ * range and LUT index; a checkerboard plan reads the grid with the same
+ * (-1)^(x+y+z) signs). */
+int fr_degrid(fr_plan plan, const float *d_grid, int channels, float *d_kdata, void *stream);
+/* Real-valued gridding of per-sample weights into G^d floats (no DCF). */
+int fr_grid_real(fr_plan plan, const float *d_w, float *d_grid, void *stream);
+/* Pipe-Menon iterative DCF (MRM 41:179, 1999): `iterations` times
+ * w <- w / degrid(grid(w)) on the plan's kernel; d_dcf holds the initial
+ * weights (e.g. all 1) and receives the result.  Samples whose degridded
+ * value is not positive keep their weight.  Stream-ordered, no host sync. */
+int fr_dcf_pipe(fr_plan plan, int iterations, float *d_dcf, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Learned DCF.  No counterpart in the reference.  A small network maps
+ * sample-density features to log-DCF; it is trained on Pipe-Menon weights
+ * (fr_dcf_pipe), which remain its fallback and its reference.
+ * ---------------------------------------------------------------------- */
+/* Density counts: each sample binned to its nearest cell (floor(x + 0.5) of
+ * the plan's normalised coordinate, clamped); d_counts[s][k] (n x nradii
+ * ints) = samples whose cell lies in the (2 r_k + 1)^d box around the cell
+ * of s, clipped to the grid.  1 <= nradii <= 8.  Exact integers. */
+int fr_density_counts(fr_plan plan, const int *radii, int nradii, int *d_counts, void *stream);
+/* Network inputs, n x (nradii + 1) floats: log(count_k / (2 r_k + 1)^d) per
+ * radius, then log(|k| / kmax + 1/1024) of the RAW coordinates (kmax <= 0:
+ * the largest |k| of the trajectory, found on the device). */
+int fr_dcf_features(fr_plan plan, const int *d_counts, const float *d_raw_traj, const int *radii, int nradii,
+                    float kmax, float *d_features, void *stream);
+
+/* The network: 5 -> 64 -> 64 -> 1, tanh hidden layers, BF16 parameters,
+ * FP32 arithmetic.  Parameter layout (FR_MLP_PARAMS values):
+ * W1[64][5] | b1[64] | W2[64][64] | b2[64] | W3[64] | b3. */
+#define FR_MLP_IN 5
+#define FR_MLP_HIDDEN 64
+#define FR_MLP_PARAMS (64 * 5 + 64 + 64 * 64 + 64 + 64 + 1)
+#define FR_MLP_EXP 1u /* write exp(output): the DCF instead of its log */
+int fr_mlp_forward(const void *d_params_bf16, const float *d_features, size_t n, unsigned flags, float *d_out,
+                   void *stream);
+/* Workspace (16-byte aligned) for fr_mlp_backward on a batch of n samples. */
+size_t fr_mlp_workspace_bytes(size_t n);
+/* Weighted mean squared error (1/n) sum_s c_s (y_s - t_s)^2 of the output
+ * against d_target over the batch (d_weight = NULL: all c_s = 1), and its
+ * gradient with respect to the parameters (FR_MLP_PARAMS floats; the
+ * reduction order is fixed, so the result is deterministic). */
+int fr_mlp_backward(const void *d_params_bf16, const float *d_features, const float *d_target,
+                    const float *d_weight, size_t n, void *d_workspace, float *d_grad, float *d_loss, void *stream);
+/* One Adam step (step >= 1) on the FP32 master parameters; refreshes the
+ * BF16 copy. */
+int fr_mlp_adam(float *d_master, void *d_params_bf16, const float *d_grad, float *d_m, float *d_v, int count,
+                float lr, float beta1, float beta2, float eps, int step, void *stream);
+int fr_mlp_to_bf16(const float *d_master, void *d_params_bf16, int count, void *stream);
+
+/* ------------------------------------------------------------------------
  * FFT stage: cuFFT::plan / cuFFT::excute (ImageFilter/cuFFT.cpp:15-37),
  * ImageFilter::fftPlan / fftExecute (ImageFilter.cpp:211-229).
  * In-place unnormalised C2C transform of `batch` contiguous images;

@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-* ``build_oracle()`` compiles the plain-C restatement ``fr_oracle.c`` into
+* ``build_oracle()`` compiles the plain-C restatement ``fr_oracle.c`` (and
+  ``fr_oracle_ext.c``, the components with no reference counterpart) into
   ``oracle/_build/liboracle.so`` (gcc, OpenMP, ``-ffp-contract=off``).
 * ``build_ref()`` compiles the reference's OWN CPU sources, where they lie in
   the reference checkout, against the stub headers in ``oracle/ref_shim``
@@ -51,14 +52,14 @@ def ref_lib_path() -> str:
 
 def build_oracle(force: bool = False) -> str:
     out = oracle_lib_path()
-    src = os.path.join(HERE, "fr_oracle.c")
+    srcs = [os.path.join(HERE, "fr_oracle.c"), os.path.join(HERE, "fr_oracle_ext.c")]
     hdr = os.path.join(HERE, "fr_oracle.h")
     if (not force and os.path.exists(out)
-            and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(out) >= max(map(os.path.getmtime, srcs + [hdr]))):
         return out
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = out + ".tmp"
-    _run(["gcc", "-std=c11", *COMMON_FLAGS, "-shared", src, "-o", tmp, "-lm"])
+    _run(["gcc", "-std=c11", *COMMON_FLAGS, "-shared", *srcs, "-o", tmp, "-lm"])
     os.replace(tmp, out)
     return out
 

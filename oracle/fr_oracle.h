@@ -126,6 +126,49 @@ int orc_recon(float *traj, const float *dcf, const float *kdata, size_t n, int c
               int dim, unsigned reconSize, float os, float kWidth, int klength,
               const unsigned *recon, float *out_mag, int threads);
 
+/* ---- fr_oracle_ext.c: components with no counterpart in the reference ---- */
+
+/* |k|^power of the raw coordinates: |k| = sqrt(sum x_d^2) in double; power 1
+ * gives |k|, power 2 gives |k|*|k|, otherwise pow(|k|, power); rounded to float. */
+void orc_dcf_analytic(const float *traj, size_t n, int dim, double power, float *out);
+
+/* Degridding (interpolation), the adjoint of gridding without DCF:
+ * out[c][s] = sum over the sample's valid taps of lut[ki] * grid[c][cell].
+ * grid: channels x G^d complex (double pairs); out: channels x n complex. */
+void orc_degrid_f64(const float *traj, size_t n, int dim, unsigned G, float kWidth, const float *lut,
+                    int klength, const double *grid, int channels, double *out);
+
+/* Real-valued gridding of weights w (no DCF) into grid (G^d doubles). */
+void orc_grid_real_f64(const float *traj, const double *w, size_t n, int dim, unsigned G, float kWidth,
+                       const float *lut, int klength, double *grid);
+
+/* Pipe-Menon iteration, `iterations` times: w <- w / degrid(grid(w)); samples
+ * whose degridded value is not positive keep their weight.  w in/out. */
+int orc_dcf_pipe_f64(const float *traj, size_t n, int dim, unsigned G, float kWidth, const float *lut,
+                     int klength, int iterations, double *w);
+
+/* Sample-density counts: every sample is binned to its nearest cell
+ * (floor(x + 0.5), clamped to the grid); counts[s][k] = samples whose cell
+ * lies in the (2 r_k + 1)^d box around the cell of s, clipped to the grid. */
+int orc_density_counts(const float *traj, size_t n, int dim, unsigned G, const int *radii, int nradii,
+                       int *counts);
+
+/* Network inputs: log(count_k / (2 r_k + 1)^d) for each radius, then
+ * log(|k| / kmax + 1/1024) of the raw coordinates.  feat: n x (nradii + 1). */
+void orc_dcf_features(const int *counts, const float *raw_traj, size_t n, int dim, const int *radii, int nradii,
+                      float kmax, float *feat);
+
+/* DCF network: 5 -> 64 -> 64 -> 1, tanh, predicting log-DCF.
+ * Parameters (float): W1[64][5] | b1[64] | W2[64][64] | b2[64] | W3[64] | b3. */
+#define ORC_MLP_IN 5
+#define ORC_MLP_HIDDEN 64
+#define ORC_MLP_PARAMS (64 * 5 + 64 + 64 * 64 + 64 + 64 + 1)
+void orc_mlp_forward(const float *params, const float *x, size_t n, double *y);
+/* Weighted mean squared error (1/n) sum c_s (y_s - t_s)^2 (weight NULL: c = 1)
+ * and its gradient (ORC_MLP_PARAMS doubles). */
+double orc_mlp_backward(const float *params, const float *x, const float *target, const float *weight, size_t n,
+                        double *grad);
+
 #ifdef __cplusplus
 }
 #endif

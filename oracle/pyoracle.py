@@ -191,6 +191,88 @@ class Oracle:
         assert rc == 0
         return out
 
+    # -- components with no reference counterpart (fr_oracle_ext.c) ---------
+    MLP_IN, MLP_HIDDEN = 5, 64
+    MLP_PARAMS = 64 * 5 + 64 + 64 * 64 + 64 + 64 + 1
+
+    def _ext_sigs(self):
+        lib = self.lib
+        if getattr(self, "_ext", False):
+            return lib
+        lib.orc_dcf_analytic.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_double, _f32p]
+        lib.orc_degrid_f64.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _f32p, C.c_int, _f64p,
+                                       C.c_int, _f64p]
+        lib.orc_grid_real_f64.argtypes = [_f32p, _f64p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _f32p, C.c_int,
+                                          _f64p]
+        lib.orc_dcf_pipe_f64.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, C.c_float, _f32p, C.c_int, C.c_int,
+                                         _f64p]
+        lib.orc_density_counts.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, _i32p, C.c_int, _i32p]
+        lib.orc_dcf_features.argtypes = [_i32p, _f32p, C.c_size_t, C.c_int, _i32p, C.c_int, C.c_float, _f32p]
+        lib.orc_mlp_forward.argtypes = [_f32p, _f32p, C.c_size_t, _f64p]
+        lib.orc_mlp_backward.argtypes = [_f32p, _f32p, _f32p, C.c_void_p, C.c_size_t, _f64p]
+        lib.orc_mlp_backward.restype = C.c_double
+        self._ext = True
+        return lib
+
+    def dcf_analytic(self, traj4, dim, power):
+        t = np.ascontiguousarray(traj4, np.float32)
+        out = np.zeros(t.shape[0], np.float32)
+        self._ext_sigs().orc_dcf_analytic(t, t.shape[0], dim, float(power), out)
+        return out
+
+    def degrid_f64(self, traj_norm4, grid, dim, G, W, lut):
+        t = np.ascontiguousarray(traj_norm4, np.float32)
+        g = np.ascontiguousarray(grid, np.complex128).reshape(-1, cells_of(dim, G))
+        out = np.zeros((g.shape[0], t.shape[0]), np.complex128)
+        self._ext_sigs().orc_degrid_f64(t, t.shape[0], dim, G, W, np.ascontiguousarray(lut, np.float32), len(lut),
+                                        g.view(np.float64).ravel(), g.shape[0], out.view(np.float64).ravel())
+        return out
+
+    def grid_real_f64(self, traj_norm4, w, dim, G, W, lut):
+        t = np.ascontiguousarray(traj_norm4, np.float32)
+        out = np.zeros(cells_of(dim, G), np.float64)
+        self._ext_sigs().orc_grid_real_f64(t, np.ascontiguousarray(w, np.float64), t.shape[0], dim, G, W,
+                                           np.ascontiguousarray(lut, np.float32), len(lut), out)
+        return out
+
+    def dcf_pipe_f64(self, traj_norm4, dim, G, W, lut, iterations, w0=None):
+        t = np.ascontiguousarray(traj_norm4, np.float32)
+        w = np.ones(t.shape[0], np.float64) if w0 is None else np.array(w0, np.float64, copy=True)
+        rc = self._ext_sigs().orc_dcf_pipe_f64(t, t.shape[0], dim, G, W, np.ascontiguousarray(lut, np.float32),
+                                               len(lut), iterations, w)
+        assert rc == 0
+        return w
+
+    def density_counts(self, traj_norm4, dim, G, radii):
+        t = np.ascontiguousarray(traj_norm4, np.float32)
+        r = np.ascontiguousarray(radii, np.int32)
+        out = np.zeros((t.shape[0], len(r)), np.int32)
+        assert self._ext_sigs().orc_density_counts(t, t.shape[0], dim, G, r, len(r), out) == 0
+        return out
+
+    def dcf_features(self, counts, raw_traj4, dim, radii, kmax):
+        c = np.ascontiguousarray(counts, np.int32)
+        r = np.ascontiguousarray(radii, np.int32)
+        out = np.zeros((c.shape[0], len(r) + 1), np.float32)
+        self._ext_sigs().orc_dcf_features(c, np.ascontiguousarray(raw_traj4, np.float32), c.shape[0], dim, r, len(r),
+                                          float(kmax), out)
+        return out
+
+    def mlp_forward(self, params, x):
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros(x.shape[0], np.float64)
+        self._ext_sigs().orc_mlp_forward(np.ascontiguousarray(params, np.float32), x, x.shape[0], out)
+        return out
+
+    def mlp_backward(self, params, x, target, weight=None):
+        x = np.ascontiguousarray(x, np.float32)
+        g = np.zeros(self.MLP_PARAMS, np.float64)
+        w = None if weight is None else np.ascontiguousarray(weight, np.float32)
+        loss = self._ext_sigs().orc_mlp_backward(np.ascontiguousarray(params, np.float32), x,
+                                                 np.ascontiguousarray(target, np.float32),
+                                                 None if w is None else w.ctypes.data, x.shape[0], g)
+        return loss, g
+
 
 class RefLib:
     """The reference's own CPU sources, compiled with stub headers."""

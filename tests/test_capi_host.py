@@ -11,7 +11,7 @@ from conftest import GOLDEN, ROOT
 
 def header_symbols():
     text = open(os.path.join(ROOT, "include", "fastrecon_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|long long|const char \*)\s*(fr_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|size_t|const char \*)\s*(fr_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
