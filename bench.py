@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="kooshball3d")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched-spiral and learned-vs-Pipe DCF measurements")
     ap.add_argument("--profile", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (ncu --profile-from-start off)")
     return ap.parse_args()
@@ -388,6 +390,17 @@ def run_ours(args, w):
         full, desc, _ = cpu_step(w, ctraj, cdcf, ckd, min(C, ncpu), ncpu, frac, fft_coils)
         line["cpu_baseline"] = {"value": N * C / full / 1e6, "unit": UNIT, "cores": ncpu, "kind": "port",
                                 "sample": desc, "ms_per_step": full * 1e3}
+    if not args.no_extras and ws == 1:
+        import bench_extras
+        del rec, traj, dcf, kd
+        torch.cuda.empty_cache()
+        for key, fn in (("batched_spiral", bench_extras.batched_spiral),
+                        ("learned_dcf", bench_extras.learned_vs_pipe)):
+            try:
+                line[key] = fn(torch)
+            except Exception as e:  # reported, not fatal: the headline line stands
+                line[key] = {"error": f"{type(e).__name__}: {e}"}
+            torch.cuda.empty_cache()
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

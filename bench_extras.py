@@ -1,0 +1,154 @@
+"""Secondary measurements reported inside bench.py's JSON line.
+
+* batched_spiral: 2D dynamic spiral, 64 frames with a seeded uneven count of
+  4-24 variable-density interleaves x 2048 samples, 12 coils, 192^2 matrix at
+  oversampling 2 (384^2 grid).  All frames gridded by one persistent launch
+  replayed from a captured CUDA graph; tile shape, bin chunk and coil group
+  from the autotuner.  value = samples x coils gridded per second.
+* learned_dcf: 3D kooshball volumes with seeded uneven spoke counts
+  (golden means, 256 samples per spoke), 32 coils, oversampling 1.25
+  (320^3 grid), 256^3 SoS.  The same batch is reconstructed end to end by
+  one captured graph with (a) the learned DCF (density features + network)
+  and (b) the Pipe-Menon DCF (20 grid/degrid iterations), and the image
+  NRMSE of (a) against (b) is reported next to the time ratio.
+
+Synthetic, seeded inputs stand in for scanner data (none ships with the
+reference): analytic k-space of a Gaussian-ellipsoid phantom times Gaussian
+coil maps with 1 % noise (fastrecon_gb300.synth).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+
+
+def _ms(torch, fn, steps, warmup, stream):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def batched_spiral(torch, steps=20, warmup=3, frames=64, coils=12, recon=192, os_=2.0, samples=2048, seed=3):
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import batch as fb
+    from fastrecon_gb300 import synth
+    rng = np.random.default_rng(seed)
+    inter = rng.integers(4, 25, frames)
+    trajs = [synth.spiral_2d(int(k), samples, rotation=float(rng.uniform(0, 2 * np.pi))) for k in inter]
+    counts = [t.shape[0] for t in trajs]
+    traj = torch.from_numpy(np.concatenate(trajs)).cuda()
+    dcf = fr.dcf_analytic(traj, 2, 1.0)
+    kd = torch.cat([synth.kspace(t, 2, recon, coils, seed=seed + f, xp=torch, device="cuda").reshape(-1)
+                    for f, t in enumerate(trajs)])
+    G = fr.grid_size(recon, os_)
+    t0 = time.perf_counter()
+    tuned, tune_ms = fb.autotune(2, G, traj, counts, kd, dcf, coils, overgrid_factor=os_, repeats=3)
+    tune_s = time.perf_counter() - t0
+    tuned.set_trajectories(traj, counts)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        out = tuned.capture(kd, dcf, coils, stream=s)
+        l0 = fr.kernel_launches()
+        ms = _ms(torch, lambda: tuned.replay(stream=s), steps, warmup, s)
+        launches = (fr.kernel_launches() - l0) / (steps + warmup)
+    del out
+    n = int(sum(counts))
+    d = tuned.desc
+    return {"value": n * coils / (ms / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_batch": ms, "frames": frames,
+            "samples": n, "coils": coils, "grid": G,
+            "autotune": {"tile": [d.tile[0], d.tile[1]], "chunk": d.chunk, "coil_group": d.coil_group,
+                         "best_ms": tune_ms, "seconds": round(tune_s, 2)},
+            "graph_replays_per_batch": launches,
+            "workload": f"2D dynamic spiral: {frames} frames x 4-24 variable-density interleaves x {samples} "
+                        f"samples (seeded), {coils} coils, {recon}^2 matrix, os {os_} -> {G}^2 grid; one "
+                        "persistent launch per batch, replayed from a CUDA graph; tiling from the autotuner"}
+
+
+def _nrmse(torch, a, ref):
+    a = a.double().flatten()
+    ref = ref.double().flatten()
+    c = (a @ ref) / (a @ a)
+    return float((c * a - ref).norm() / ref.norm())
+
+
+def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os_=1.25, readout=256,
+                    spoke_range=(10_000, 60_000), seed=5, model=None):
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import learned_dcf as ld
+    from fastrecon_gb300 import synth
+    model = model or os.path.join(ROOT, "fastrecon_gb300", "models", "dcf_mlp_3d.npz")
+    if not os.path.exists(model):
+        return {"unavailable": "no trained 3D DCF model (python -m fastrecon_gb300.train_dcf --dim 3)"}
+    net = ld.DCFNet.load(model)
+    rng = np.random.default_rng(seed)
+    spokes = rng.integers(spoke_range[0], spoke_range[1] + 1, volumes)
+    G = fr.grid_size(recon, os_)
+    lut = fr.kb_lut(4.0, os_, 512)
+    scale = math.exp(-ld.target_offset(lut, 4.0, 3))
+    vols = []
+    for v, sp in enumerate(spokes):
+        t = synth.kooshball_3d(int(sp), readout)
+        td = torch.from_numpy(t).cuda()
+        plan = fr.GridPlan(3, G, 4.0, lut=lut, checkerboard=True)
+        plan.set_trajectory(td)
+        kd = synth.kspace(t, 3, recon, coils, seed=seed + v, xp=torch, device="cuda")
+        vols.append(dict(traj=td, plan=plan, kd=kd, n=t.shape[0],
+                         w=torch.empty(t.shape[0], dtype=torch.float32, device="cuda"),
+                         feat=torch.empty((t.shape[0], 5), dtype=torch.float32, device="cuda"),
+                         cnt=torch.empty((t.shape[0], 4), dtype=torch.int32, device="cuda")))
+    grid = torch.empty((coils, G ** 3), dtype=torch.complex64, device="cuda")
+    out_size = (recon, recon, recon)
+    fft = fr.FFT(3, (G, G, G), coils, +1)
+    img_l = torch.empty((volumes, recon ** 3), dtype=torch.float32, device="cuda")
+    img_p = torch.empty_like(img_l)
+    lib = fr.load()
+
+    def run(mode, s):
+        for i, V in enumerate(vols):
+            if mode == "learned":
+                ld.density_counts(V["plan"], ld.RADII, stream=s, out=V["cnt"])
+                ld.dcf_features(V["plan"], V["traj"], counts=V["cnt"], stream=s, out=V["feat"])
+                net.forward(V["feat"], exp=True, scale=scale, out=V["w"], stream=s)
+            else:
+                V["w"].fill_(1.0)
+                fr.capi.check(lib.fr_dcf_pipe(V["plan"].h, 20, C.c_void_p(V["w"].data_ptr()),
+                                              C.c_void_p(s.cuda_stream)), "fr_dcf_pipe")
+            V["plan"].grid(V["kd"], V["w"], out=grid, stream=s)
+            fft(grid, stream=s)  # the grid was flushed with the fftShift checkerboard
+            fr.sos(grid, 3, G, out_size, stream=s, out=(img_l if mode == "learned" else img_p)[i])
+
+    s = torch.cuda.Stream()
+    res = {}
+    for mode in ("pipe", "learned"):
+        with torch.cuda.stream(s):
+            run(mode, s)  # warm: buffers reach their size before capture
+            s.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+                run(mode, s)
+            ms = _ms(torch, g.replay, steps, warmup, s)
+        res[mode] = ms
+        del g
+    nr = [_nrmse(torch, img_l[i], img_p[i]) for i in range(volumes)]
+    n = int(sum(V["n"] for V in vols))
+    return {"learned_ms": res["learned"], "pipe_ms": res["pipe"], "speedup": res["pipe"] / res["learned"],
+            "nrmse_median": float(np.median(nr)), "nrmse_max": float(np.max(nr)), "volumes": volumes,
+            "samples": n, "coils": coils, "grid": G,
+            "workload": f"{volumes} 3D kooshball volumes, seeded {spoke_range[0]}-{spoke_range[1]} golden-means "
+                        f"spokes x {readout}, {coils} coils, os {os_} -> {G}^3 grid, {recon}^3 SoS; one captured "
+                        "graph per DCF method (DCF + grid + FFT + crop/SoS for every volume)",
+            "nrmse": "image NRMSE of the learned-DCF recon against the Pipe-DCF recon after the best scalar scale"}

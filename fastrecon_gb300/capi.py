@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libfastrecon_gb300.so")
 FR_PLAN_CHECKERBOARD = 1
 FR_RECON_DEAPODIZE = 1
 FR_RECON_CUFFT = 2
+FR_RECON_PRUNED_FFT = 4
 
 _lib = None
 
@@ -79,7 +80,7 @@ _SIGS = {
     "fr_dcf_pipe": (C.c_int, [_VP, C.c_int, _VP, _VP]),
     "fr_density_counts": (C.c_int, [_VP, C.POINTER(C.c_int), C.c_int, _VP, _VP]),
     "fr_dcf_features": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_int), C.c_int, C.c_float, _VP, _VP]),
-    "fr_mlp_forward": (C.c_int, [_VP, _VP, C.c_size_t, C.c_uint, _VP, _VP]),
+    "fr_mlp_forward": (C.c_int, [_VP, _VP, C.c_size_t, C.c_uint, C.c_float, _VP, _VP]),
     "fr_mlp_workspace_bytes": (C.c_size_t, [C.c_size_t]),
     "fr_mlp_backward": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP, _VP, _VP]),
     "fr_mlp_adam": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,

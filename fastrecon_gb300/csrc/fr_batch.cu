@@ -102,6 +102,7 @@ int fill_batch_grid(fr_batch b, BatchGrid *g)
     g->L = p->L;
     g->smax = p->lut_smax;
     g->kc = p->lut_kc;
+    g->lut_absmax = p->lut_absmax;
     g->checkerboard = (p->flags & FR_PLAN_CHECKERBOARD) ? 1 : 0;
     g->traj = b->traj.as<float4>();
     g->recs = b->recs.as<unsigned long long>();

@@ -284,6 +284,9 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         LutIndexTable lt = lut_index_table(p->hw, p->L);
         p->lut_smax = lt.smax;
         p->lut_kc = lt.kc;
+        p->lut_absmax = 0.f;
+        for (float v : p->lut) p->lut_absmax = std::max(p->lut_absmax, std::fabs(v));
+        if (!(p->lut_absmax > 0.f) || !std::isfinite(p->lut_absmax)) p->lut_absmax = 1.f;
         p->lut_entries.resize(4 * (size_t)p->L);
         for (int k = 0; k < p->L; ++k) {
             p->lut_entries[4 * k + 0] = lt.thr[k + 1];
@@ -457,11 +460,12 @@ int fr_dcf_features(fr_plan p, const int *d_counts, const float *d_raw_traj, con
                             p->small.as<unsigned>(), (cudaStream_t)stream);
 }
 
-int fr_mlp_forward(const void *d_params, const float *d_features, size_t n, unsigned flags, float *d_out, void *stream)
+int fr_mlp_forward(const void *d_params, const float *d_features, size_t n, unsigned flags, float scale, float *d_out,
+                   void *stream)
 {
     if (n && (!d_params || !d_features || !d_out)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
     if (reinterpret_cast<uintptr_t>(d_params) & 1) return fail(FR_ERR_INVALID_ARGUMENT, "parameters must be 2-byte aligned");
-    return mlp_forward_run(d_params, d_features, n, (flags & FR_MLP_EXP) ? 1 : 0, d_out, (cudaStream_t)stream);
+    return mlp_forward_run(d_params, d_features, n, (flags & FR_MLP_EXP) ? 1 : 0, scale, d_out, (cudaStream_t)stream);
 }
 
 size_t fr_mlp_workspace_bytes(size_t n) { return mlp_workspace_bytes(n); }

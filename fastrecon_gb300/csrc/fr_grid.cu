@@ -51,6 +51,7 @@ struct GridParams {
     long long grid_frame_floats;
     int *work_counter;  // persistent kernel: next work index
     long long nwork;    // persistent kernel: nitems * ngroups
+    float lut_absmax;   // max |lut[k]|: bounds every tap weight
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -72,9 +73,24 @@ __device__ __forceinline__ unsigned smem_addr(const void *p)
 {
     return (unsigned)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void red_add(unsigned a, float v)
+// Fixed-point accumulation: a float shared-memory add is a compare-and-swap
+// loop on this GPU, an integer add is one native instruction.  Each tap adds
+// round(w * v * S) (S a power of two chosen per work item and coil float so
+// that no partial sum can leave the int32 range, see grid_item); the float
+// value is acc / S at the flush.
+__device__ __forceinline__ void red_add_fx(unsigned a, float w, float vs)
 {
-    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+    // w * vs rounded to the nearest integer: |w * vs| < 2^22, so adding
+    // 1.5 * 2^23 in the same fused operation lands in [2^23, 2^24), where the
+    // float spacing is 1, and the low mantissa bits are the integer.
+    const int i = __float_as_int(fmaf(w, vs, 12582912.f)) - 0x4B400000;
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(i) : "memory");
+}
+__device__ __forceinline__ int2 lds_i32x2(unsigned a)
+{
+    int2 r;
+    asm volatile("ld.shared.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "r"(a) : "memory");
+    return r;
 }
 __device__ __forceinline__ int4 lds_s32x4(unsigned a)
 {
@@ -100,12 +116,6 @@ __device__ __forceinline__ float4 lds_f32x4(unsigned a)
                  : "memory");
     return r;
 }
-__device__ __forceinline__ float2 lds_f32x2(unsigned a)
-{
-    float2 r;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(a) : "memory");
-    return r;
-}
 __device__ __forceinline__ void sts_s32x2(unsigned a, int2 v)
 {
     asm volatile("st.shared.v2.s32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
@@ -122,7 +132,7 @@ __device__ __forceinline__ unsigned lds_u8(unsigned a)
 // (even tile x extent and grid size), rows advance without divisions.
 template <int R>
 __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gridf, unsigned acc, int cg, int ox, int oy,
-                                                 int oz, bool zero)
+                                                 int oz, bool zero, const float *inv_scale)
 {
     const int CG = P.coil_group;
     const int Tx = P.tile[0], Ty = P.tile[1], Tz = P.tile[2];
@@ -141,6 +151,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
         const bool xin = gx < P.G;  // gx even, G even: gx + 1 < G as well
         for (int cl = 0; cl < ncl; ++cl) {
             float4 *gridc = reinterpret_cast<float4 *>(gridf + 2 * (size_t)(cg * CG + cl) * cells);
+            const float ir = zero ? 0.f : inv_scale[2 * cl], ii = zero ? 0.f : inv_scale[2 * cl + 1];
             int ly = rr0 % Ty, lz = rr0 / Ty;
             for (int r = rr0; r < rows; r += rstep) {
                 const int gy = oy + ly, gz = oz + lz;
@@ -148,9 +159,9 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
                     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (!zero) {
                         const int i = r * Tx + lx;
-                        const float2 a = lds_f32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
-                        const float2 b = lds_f32x2(acc + 4u * (unsigned)((i + 1) * R + ((2 * cl) ^ swz<R>(i + 1))));
-                        v = make_float4(a.x, a.y, b.x, b.y);
+                        const int2 a = lds_i32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
+                        const int2 b = lds_i32x2(acc + 4u * (unsigned)((i + 1) * R + ((2 * cl) ^ swz<R>(i + 1))));
+                        v = make_float4((float)a.x * ir, (float)a.y * ii, (float)b.x * ir, (float)b.y * ii);
                         if (P.checkerboard) {  // (-1)^(x+y+z): opposite signs for x and x+1
                             if ((gx + gy + gz) & 1) {
                                 v.x = -v.x;
@@ -186,7 +197,8 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
         if (gx >= P.G || gy >= P.G || gz >= Gz) continue;
         float2 v = make_float2(0.f, 0.f);
         if (!zero) {
-            v = lds_f32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
+            const int2 a = lds_i32x2(acc + 4u * (unsigned)(i * R + ((2 * cl) ^ swz<R>(i))));
+            v = make_float2((float)a.x * inv_scale[2 * cl], (float)a.y * inv_scale[2 * cl + 1]);
             if (P.checkerboard && ((gx + gy + gz) & 1)) {
                 v.x = -v.x;
                 v.y = -v.y;
@@ -199,9 +211,10 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
 
-// Shared-memory layout of the scatter: accumulator tile [K][R] floats | LUT
+// Shared-memory layout of the scatter: accumulator tile [K][R] int32 | LUT
 // entries [L] float4 | per warp two tap-list buffers [32] {byte offset of the
-// tap's cell row (swizzled), weight} | tap decode table [16][64] bytes.
+// tap's cell row (swizzled), weight} | tap decode table [16][64] bytes |
+// per coil float: bound sum, bound max, inverse scale [3][64] floats.
 template <int R>
 __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
 {
@@ -241,12 +254,18 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     const float4 *traj = P.traj + s_off;
     const float *dcf = P.dcf + s_off;
 
+    float *bsum_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + (size_t)K * R * 4 +
+                                              (size_t)P.L * 16 + kWarps * 2 * kListEntries * 8 + 16 * 64);
+    unsigned *bmax_s = reinterpret_cast<unsigned *>(bsum_s + 64);
+    float *inv_s = bsum_s + 128;
+
     if (it.count == 0) {  // empty tile: stream zeros
-        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, true);
+        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, true, inv_s);
         return;
     }
 
     for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) bsum_s[i] = 0.f;  // bsum_s and bmax_s
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
@@ -275,6 +294,58 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     }
     const unsigned long long *recs = P.recs + it.begin;
 
+    // Scale of the fixed-point tile, per coil float f: with B_f = sum and
+    // M_f = max over the item's samples of |dcf * k_f|, and |w| <= lut_absmax,
+    // every partial sum is below B_f * lut_absmax and every add below
+    // M_f * lut_absmax, so S_f = the largest power of two with
+    // S_f * B_f * lut_absmax <= 2^30 and S_f * M_f * lut_absmax <= 2^21 keeps
+    // the tile in int32 and each add exact to +-1/2.  The rounding error of
+    // an add is then at most B_f / 2^31 (dense items) or 2^-23 M_f.
+    {
+        float bs[NF], bm[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) bs[k] = bm[k] = 0.f;
+        for (int j = warp; j < it.count; j += kWarps) {
+            const unsigned long long rec = recs[j];
+            const unsigned box = (unsigned)(rec >> 32);
+            if (((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) == 0) continue;
+            const unsigned s = (unsigned)rec;
+            const float d = dcf[s];
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                const float a = coil_ok[k] ? fabsf(__fmul_rn(d, kdf[k][2 * (size_t)s])) : 0.f;
+                bs[k] += a;
+                bm[k] = fmaxf(bm[k], a);
+            }
+        }
+        if (q == 0) {
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                if (coil_ok[k]) {
+                    atomicAdd(&bsum_s[f0 + 32 * k], bs[k]);
+                    atomicMax(&bmax_s[f0 + 32 * k], __float_as_uint(bm[k]));
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < R) {
+            const float B = __fmul_rn(bsum_s[threadIdx.x], P.lut_absmax);
+            const float M = __fmul_rn(__uint_as_float(bmax_s[threadIdx.x]), P.lut_absmax);
+            int e = 0;
+            if (B > 0.f && M > 0.f) {
+                // largest power of two 2^e <= min(2^30 / B, 2^21 / M)
+                const float t = fminf(__fdiv_rn(1073741824.f, B), __fdiv_rn(2097152.f, M));
+                frexpf(t, &e);
+                e = max(min(e - 1, 100), -100);
+            }
+            inv_s[threadIdx.x] = ldexpf(1.f, -e);  // exact: a power of two
+        }
+        __syncthreads();
+    }
+    float sc[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) sc[k] = __fdiv_rn(1.f, inv_s[f0 + 32 * k]);  // exact
+
     for (int j = warp; j < it.count; j += kWarps) {
         const unsigned long long rec = recs[j];
         const unsigned s = (unsigned)rec;
@@ -290,7 +361,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         float val[NF];
 #pragma unroll
         for (int k = 0; k < NF; ++k)
-            val[k] = coil_ok[k] ? __fmul_rn(d, kdf[k][2 * (size_t)s]) : 0.f;  // GridLut.cpp:109
+            val[k] = coil_ok[k] ? __fmul_rn(__fmul_rn(d, kdf[k][2 * (size_t)s]), sc[k]) : 0.f;  // GridLut.cpp:109, scaled
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
         const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64);
         const int nround = (ntap + 31) >> 5;
@@ -346,8 +417,8 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
 #pragma unroll
                     for (int kk = 0; kk < NF; ++kk) {
                         if (coil_ok[kk]) {
-                            red_add(a0 + 128u * kk, __fmul_rn(__int_as_float(e2.y), val[kk]));
-                            red_add(a1 + 128u * kk, __fmul_rn(__int_as_float(e2.w), val[kk]));
+                            red_add_fx(a0 + 128u * kk, __int_as_float(e2.y), val[kk]);
+                            red_add_fx(a1 + 128u * kk, __int_as_float(e2.w), val[kk]);
                         }
                     }
                 }
@@ -356,12 +427,12 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
                     const unsigned a0 = acc + ((unsigned)e1.x ^ f0b);
 #pragma unroll
                     for (int kk = 0; kk < NF; ++kk)
-                        if (coil_ok[kk]) red_add(a0 + 128u * kk, __fmul_rn(__int_as_float(e1.y), val[kk]));
+                        if (coil_ok[kk]) red_add_fx(a0 + 128u * kk, __int_as_float(e1.y), val[kk]);
                 }
             } else {
                 for (int k = q; k < n; k += NG) {
                     const int2 e1 = lds_s32x2(lst + 8u * k);
-                    if (coil_ok[0]) red_add(acc + ((unsigned)e1.x ^ f0b), __fmul_rn(__int_as_float(e1.y), val[0]));
+                    if (coil_ok[0]) red_add_fx(acc + ((unsigned)e1.x ^ f0b), __int_as_float(e1.y), val[0]);
                 }
             }
         }
@@ -369,11 +440,18 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     __syncthreads();
 
     if (it.slot < 0) {
-        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, false);
+        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, false, inv_s);
     } else {
+        // partial tile as floats, same swizzled [cell][coil float] layout
         float4 *dst = reinterpret_cast<float4 *>(
             P.partials + ((size_t)it.slot * P.ngroups + cg) * (size_t)K * R);
-        for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) dst[i] = smem4[i];
+        const int4 *src = reinterpret_cast<const int4 *>(smem4);
+        for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) {
+            const int cell = (4 * i) / R, p0 = (4 * i) % R, sw = swz<R>(cell);
+            const int4 a = src[i];
+            dst[i] = make_float4((float)a.x * inv_s[p0 ^ sw], (float)a.y * inv_s[(p0 + 1) ^ sw],
+                                 (float)a.z * inv_s[(p0 + 2) ^ sw], (float)a.w * inv_s[(p0 + 3) ^ sw]);
+        }
     }
 }
 
@@ -494,7 +572,7 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
 size_t grid_smem_bytes(long long K, int R, int L)
 {
     // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode table
-    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64;
+    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64 + 3 * 64 * 4;
 }
 
 int floats_per_cell(int coil_group)
@@ -548,6 +626,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.L = p->L;
     P.smax = p->lut_smax;
     P.kc = p->lut_kc;
+    P.lut_absmax = p->lut_absmax;
     P.khalf = 0.25f;  // 0.5 - slack 0.25: the guess is the exact index or one below
     P.checkerboard = (p->flags & FR_PLAN_CHECKERBOARD) ? 1 : 0;
     P.frame_off = nullptr;
@@ -636,6 +715,7 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.L = gi.L;
     P.smax = gi.smax;
     P.kc = gi.kc;
+    P.lut_absmax = gi.lut_absmax;
     P.khalf = 0.25f;
     P.checkerboard = 0;
     P.frame_off = nullptr;
@@ -746,6 +826,7 @@ int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf,
     P.L = b.L;
     P.smax = b.smax;
     P.kc = b.kc;
+    P.lut_absmax = b.lut_absmax;
     P.khalf = 0.25f;
     P.checkerboard = b.checkerboard;
     P.frame_off = b.frame_off;

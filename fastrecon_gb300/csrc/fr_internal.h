@@ -88,6 +88,7 @@ struct fr_plan_s {
     fr::DevBuf lut_e;         // L float4 {thr[k+1], lut[k], lut[k+1], 0}
     std::vector<float> lut_entries;
     float lut_smax = 0.f, lut_kc = 0.f;
+    float lut_absmax = 1.f;   // max |lut[k]| (bounds every tap weight)
     fr::DevBuf traj;          // n float4, normalised
     fr::DevBuf bounds;        // 16 floats: raw lo/hi as ordered ints, tr, scale, norm lo/hi
     fr::DevBuf tile_count;    // ntiles int
@@ -182,6 +183,7 @@ struct GridInto {
     int coil_group;
     int L;
     float smax, kc;
+    float lut_absmax;
     const float4 *traj;
     const unsigned long long *recs;
     const WorkItem *items;
@@ -201,6 +203,7 @@ struct BatchGrid {
     int coil_group;
     int L;
     float smax, kc;
+    float lut_absmax;
     int checkerboard;
     const float4 *traj;               // all frames, normalised, concatenated
     const unsigned long long *recs;   // all frames' bin records (frame-local sample index)
@@ -233,7 +236,8 @@ int density_counts_run(fr_plan p, const int *radii, int nradii, int *d_counts, c
 int dcf_features_run(const int *d_counts, const float *d_raw, size_t n, int dim, const int *radii, int nradii,
                      float kmax, float *d_feat, unsigned *d_scratch, cudaStream_t s);
 size_t mlp_workspace_bytes(size_t n);
-int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, float *d_y, cudaStream_t s);
+int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, float scale, float *d_y,
+                    cudaStream_t s);
 int mlp_backward_run(const void *d_params, const float *d_x, const float *d_t, const float *d_w, size_t n, void *ws,
                      float *d_grad, float *d_loss, cudaStream_t s);
 int mlp_adam_run(float *d_master, void *d_params, const float *d_grad, float *d_m, float *d_v, int count, float lr,

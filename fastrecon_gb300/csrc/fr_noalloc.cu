@@ -164,6 +164,9 @@ extern "C" int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned 
     gi.L = L;
     gi.smax = smax;
     gi.kc = kc;
+    gi.lut_absmax = 0.f;
+    for (int k = 0; k < L; ++k) gi.lut_absmax = std::max(gi.lut_absmax, std::fabs(lut_host[k]));
+    if (!(gi.lut_absmax > 0.f) || !std::isfinite(gi.lut_absmax)) gi.lut_absmax = 1.f;
     gi.traj = pi.traj;
     gi.recs = po.recs;
     gi.items = po.items;

@@ -80,7 +80,7 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     }
     pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
     st = fr_plan_create(&pd, &r->plan);
-    if (!st && r->checkerboard && !(d->flags & FR_RECON_CUFFT)) {
+    if (!st && r->checkerboard && (d->flags & FR_RECON_PRUNED_FFT) && !(d->flags & FR_RECON_CUFFT)) {
         // the pruned transform where the grid size factors into 2, 3, 5
         if (fr_fft_crop_sos_create(d->dim, r->G, d->channels, r->d.out_size, &r->pruned) != FR_OK)
             r->pruned = nullptr;

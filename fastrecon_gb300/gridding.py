@@ -79,6 +79,7 @@ class GridPlan:
         check(self.lib.fr_plan_create(C.byref(d), C.byref(h)), "fr_plan_create")
         self.h = h
         self.dim, self.G, self.n = dim, grid_size, 0
+        self.W = kernel_width
 
     def __del__(self):
         if getattr(self, "h", None) is not None and self.h.value:
@@ -234,11 +235,12 @@ def crop(imgs, dim: int, G: int, crop_size, stream=None):
     return out
 
 
-def sos(imgs, dim: int, G: int, recon, deapod=None, stream=None):
+def sos(imgs, dim: int, G: int, recon, deapod=None, stream=None, out=None):
     """ImageFilter::SOS(reconSize) then |.|: (C, G^d) complex64 -> recon float32."""
     torch = _torch()
     rs = list(recon) + [1] * (3 - len(recon))
-    out = torch.empty(int(np.prod(rs)), dtype=torch.float32, device="cuda")
+    if out is None:
+        out = torch.empty(int(np.prod(rs)), dtype=torch.float32, device="cuda")
     lib = capi.load()
     check(lib.fr_sos(_ptr(imgs), imgs.shape[0], dim, u3(_size3(dim, G)), u3(rs), _ptr(deapod), _ptr(out),
                      C.c_void_p(_stream(stream))), "fr_sos")
@@ -289,9 +291,10 @@ class CropSoS:
             self.lib.fr_fft_crop_sos_destroy(self.h)
             self.h = None
 
-    def __call__(self, grid, deapod=None, stream=None):
+    def __call__(self, grid, deapod=None, stream=None, out=None):
         torch = _torch()
-        out = torch.empty(int(np.prod(self.out_size)), dtype=torch.float32, device="cuda")
+        if out is None:
+            out = torch.empty(int(np.prod(self.out_size)), dtype=torch.float32, device="cuda")
         check(self.lib.fr_fft_crop_sos_execute(self.h, _ptr(grid), _ptr(deapod), _ptr(out),
                                                C.c_void_p(_stream(stream))), "fr_fft_crop_sos_execute")
         return out
@@ -302,7 +305,7 @@ class Recon:
 
     def __init__(self, dim: int, recon_size: int, overgrid_factor: float, channels: int, out_size=None,
                  kernel_width: float = 4.0, lut_length: int = 512, max_samples: int = 0, tile=(0, 0, 0),
-                 coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False):
+                 coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False, pruned_fft: bool = False):
         self.lib = capi.load()
         d = capi.ReconDesc()
         d.dim = dim
@@ -318,7 +321,8 @@ class Recon:
         d.channels = channels
         d.max_samples = max_samples
         d.coil_group = coil_group
-        d.flags = (capi.FR_RECON_DEAPODIZE if deapodize else 0) | (capi.FR_RECON_CUFFT if use_cufft else 0)
+        d.flags = ((capi.FR_RECON_DEAPODIZE if deapodize else 0) | (capi.FR_RECON_CUFFT if use_cufft else 0) |
+                   (capi.FR_RECON_PRUNED_FFT if pruned_fft else 0))
         h = C.c_void_p()
         check(self.lib.fr_recon_create(C.byref(d), C.byref(h)), "fr_recon_create")
         self.h = h

@@ -6,7 +6,8 @@ around each sample (from the per-cell bin counts of the plan's normalised
 trajectory) and log(|k| / max|k| + 1/1024).  Training weights each sample's
 squared log-DCF error by (w^2 E)^(1/4), w its Pipe-Menon weight and E the
 mean k-space energy of a synthetic object there, so that the fit is best
-where DCF errors reach the image.  The network is trained on Pipe-Menon weights
+where DCF errors reach the image; the target is normalised by the kernel
+mass (target_offset) so that grids of different oversampling agree.  The network is trained on Pipe-Menon weights
 computed on the GPU (``GridPlan.dcf_pipe``); those weights remain its
 fallback and the reference its images are judged against.
 
@@ -41,22 +42,24 @@ def _radii_arg(radii):
     return r, len(radii)
 
 
-def density_counts(plan: GridPlan, radii=RADII, stream=None):
+def density_counts(plan: GridPlan, radii=RADII, stream=None, out=None):
     """(n, len(radii)) int32: samples in the (2r+1)^d box around each sample's cell."""
     torch = _torch()
-    out = torch.empty((plan.n, len(radii)), dtype=torch.int32, device="cuda")
+    if out is None:
+        out = torch.empty((plan.n, len(radii)), dtype=torch.int32, device="cuda")
     r, nr = _radii_arg(radii)
     check(capi.load().fr_density_counts(plan.h, r, nr, _ptr(out), C.c_void_p(_stream(stream))), "fr_density_counts")
     return out
 
 
-def dcf_features(plan: GridPlan, raw_traj, counts=None, radii=RADII, kmax: float = 0.0, stream=None):
+def dcf_features(plan: GridPlan, raw_traj, counts=None, radii=RADII, kmax: float = 0.0, stream=None, out=None):
     """(n, len(radii) + 1) float32 network inputs for the plan's trajectory."""
     torch = _torch()
     if counts is None:
         counts = density_counts(plan, radii, stream)
     raw_traj = raw_traj.contiguous()
-    out = torch.empty((plan.n, len(radii) + 1), dtype=torch.float32, device="cuda")
+    if out is None:
+        out = torch.empty((plan.n, len(radii) + 1), dtype=torch.float32, device="cuda")
     r, nr = _radii_arg(radii)
     check(capi.load().fr_dcf_features(plan.h, _ptr(counts), _ptr(raw_traj), r, nr, float(kmax), _ptr(out),
                                       C.c_void_p(_stream(stream))), "fr_dcf_features")
@@ -96,14 +99,15 @@ class DCFNet:
     def params_bf16_as_float(self) -> np.ndarray:
         return self.bf16.float().cpu().numpy()
 
-    def forward(self, features, exp: bool = False, out=None, stream=None):
+    def forward(self, features, exp: bool = False, scale: float = 1.0, out=None, stream=None):
+        """Network output per sample, or scale * exp(output) with exp=True."""
         torch = _torch()
         features = features.contiguous()
         n = features.shape[0]
         if out is None:
             out = torch.empty(n, dtype=torch.float32, device="cuda")
-        check(self.lib.fr_mlp_forward(_ptr(self.bf16), _ptr(features), n, FR_MLP_EXP if exp else 0, _ptr(out),
-                                      C.c_void_p(_stream(stream))), "fr_mlp_forward")
+        check(self.lib.fr_mlp_forward(_ptr(self.bf16), _ptr(features), n, FR_MLP_EXP if exp else 0, float(scale),
+                                      _ptr(out), C.c_void_p(_stream(stream))), "fr_mlp_forward")
         return out
 
     def loss_grad(self, features, target, weight=None, stream=None):
@@ -163,10 +167,29 @@ def energy_weight(traj, dim, recon, w_pipe, seed=0, power=0.25):
     return (c / c.mean()).float()
 
 
+def kernel_mass(lut, kernel_width: float, dim: int, steps: int = 100000) -> float:
+    """Integral of the radial LUT kernel over the plane (2D) or space (3D),
+    with the gridding's LUT index rule: M = int K(|x|) d^d x."""
+    lut = np.asarray(lut, np.float64)
+    hw = kernel_width / 2
+    r = (np.arange(steps) + 0.5) * (hw / steps)
+    k = lut[np.minimum(np.rint(r / hw * (len(lut) - 1)).astype(np.int64), len(lut) - 1)]
+    shell = 2 * np.pi * r if dim == 2 else 4 * np.pi * r * r
+    return float(np.sum(k * shell) * (hw / steps))
+
+
+def target_offset(lut, kernel_width: float, dim: int) -> float:
+    """Pipe-Menon weights at density rho approach 1 / (rho M^2) (M the kernel
+    mass), so log w + 2 log M depends on the samples' density alone: the
+    network learns that normalised target and the DCF is exp(net) / M^2."""
+    return 2.0 * float(np.log(kernel_mass(lut, kernel_width, dim)))
+
+
 def learned_dcf(plan: GridPlan, raw_traj, net: DCFNet, kmax: float = 0.0, stream=None):
-    """DCF of the plan's trajectory from the network (exp of its output)."""
+    """DCF of the plan's trajectory from the network."""
     feats = dcf_features(plan, raw_traj, kmax=kmax, stream=stream)
-    return net.forward(feats, exp=True, stream=stream)
+    scale = float(np.exp(-target_offset(plan.lut, plan.W, plan.dim)))
+    return net.forward(feats, exp=True, scale=scale, stream=stream)
 
 
 def train(net: DCFNet, features, log_target, weight=None, steps: int = 2000, batch: int = 16384, lr: float = 3e-3,

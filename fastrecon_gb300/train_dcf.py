@@ -83,7 +83,7 @@ def evaluate(net, dim, trajs, coils=4, seed=100):
     out = []
     for i, (t, recon, os_, fam) in enumerate(trajs):
         plan, td, w_pipe, x = pipe_and_features(t, dim, recon, os_)
-        w_net = net.forward(x, exp=True)
+        w_net = net.forward(x, exp=True, scale=math.exp(-ld.target_offset(plan.lut, plan.W, dim)))
         w_plain = G_.dcf_analytic(td, dim, 1.0 if dim == 2 else 2.0)
         kd = synth.kspace(t, dim, recon, coils, seed=seed + i, xp=torch, device="cuda")
         rec = G_.Recon(dim, recon, os_, coils)
@@ -104,12 +104,12 @@ def build_dataset(dim, n_traj, seed, per_traj=20000):
     g.manual_seed(seed)
     for i in range(n_traj):
         t, recon, os_, _fam = draw_trajectory(dim, rng)
-        _, _, w, x = pipe_and_features(t, dim, recon, os_)
+        plan, _, w, x = pipe_and_features(t, dim, recon, os_)
         c = ld.energy_weight(t, dim, recon, w, seed=seed * 100003 + i)
         n = t.shape[0]
         idx = torch.randint(0, n, (min(per_traj, n),), device="cuda", generator=g)
         X.append(x[idx])
-        Y.append(torch.log(w[idx]))
+        Y.append(torch.log(w[idx]) + ld.target_offset(plan.lut, plan.W, dim))
         C.append(c[idx])
     return torch.cat(X), torch.cat(Y), torch.cat(C)
 

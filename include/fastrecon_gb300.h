@@ -264,9 +264,9 @@ int fr_dcf_features(fr_plan plan, const int *d_counts, const float *d_raw_traj, 
 #define FR_MLP_IN 5
 #define FR_MLP_HIDDEN 64
 #define FR_MLP_PARAMS (64 * 5 + 64 + 64 * 64 + 64 + 64 + 1)
-#define FR_MLP_EXP 1u /* write exp(output): the DCF instead of its log */
-int fr_mlp_forward(const void *d_params_bf16, const float *d_features, size_t n, unsigned flags, float *d_out,
-                   void *stream);
+#define FR_MLP_EXP 1u /* write scale * exp(output): the DCF instead of its log */
+int fr_mlp_forward(const void *d_params_bf16, const float *d_features, size_t n, unsigned flags, float scale,
+                   float *d_out, void *stream);
 /* Workspace (16-byte aligned) for fr_mlp_backward on a batch of n samples. */
 size_t fr_mlp_workspace_bytes(size_t n);
 /* Weighted mean squared error (1/n) sum_s c_s (y_s - t_s)^2 of the output
@@ -346,8 +346,9 @@ typedef struct fr_recon_s *fr_recon;
 
 enum {
     FR_RECON_DEAPODIZE = 1u << 0, /* divide by the kernel's image-domain apodization */
-    FR_RECON_CUFFT = 1u << 1      /* use the full cuFFT transform + SoS kernel even where the
-                                     pruned transform (fr_fft_crop_sos) applies */
+    FR_RECON_CUFFT = 1u << 1,     /* the full cuFFT transform + crop/SoS kernel (the default) */
+    FR_RECON_PRUNED_FFT = 1u << 2 /* the pruned transform with fused crop + SoS (fr_fft_crop_sos)
+                                     where it applies (even G = 2^a 3^b 5^c <= 1024) */
 };
 
 typedef struct {

@@ -11,7 +11,7 @@ import pytest
 from conftest import rel_l2
 from fastrecon_gb300 import synth
 
-TOL = 1e-6  # same kernel body; only the order of shared-memory additions differs
+TOL = 1e-5  # the project's gridding bar: batches may chunk bins differently from the single path
 
 
 def test_batch_rejects_bad_arguments_without_gpu(frlib):

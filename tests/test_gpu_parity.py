@@ -388,3 +388,13 @@ def test_recon_cufft_path_vs_reference(torch):
                      use_cufft=True)
         img = r.run(cu(torch, c["traj"]), cu(torch, c["dcf"]), cu(torch, c["kdata"])).cpu().numpy()
         assert rel_l2(img, c["image"]) <= TOL
+
+
+def test_recon_pruned_fft_path_vs_reference(torch):
+    import fastrecon_gb300 as fr
+    for name in ("radial2d_small", "koosh3d_small"):
+        c = load_case(name)
+        r = fr.Recon(c["dim"], c["recon"], c["os"], c["coils"], kernel_width=c["W"], lut_length=c["L"],
+                     pruned_fft=True)
+        img = r.run(cu(torch, c["traj"]), cu(torch, c["dcf"]), cu(torch, c["kdata"])).cpu().numpy()
+        assert rel_l2(img, c["image"]) <= TOL

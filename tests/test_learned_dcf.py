@@ -114,8 +114,8 @@ def test_gpu_mlp_forward_matches_oracle(oracle):
     got = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
     want = oracle.mlp_forward(pf, x)
     assert np.linalg.norm(got - want) <= TOL_FWD * np.linalg.norm(want)
-    gexp = net.forward(torch.from_numpy(x).cuda(), exp=True).cpu().numpy()
-    assert np.allclose(gexp, np.exp(want), rtol=1e-4)
+    gexp = net.forward(torch.from_numpy(x).cuda(), exp=True, scale=0.25).cpu().numpy()
+    assert np.allclose(gexp, 0.25 * np.exp(want), rtol=1e-4)
 
 
 @pytest.mark.gpu
@@ -190,7 +190,7 @@ def test_gpu_learned_dcf_beats_plain_method():
         plan, td = _plan_for(fr, torch, t, 2, G, W, os_)
         w = plan.dcf_pipe(20)
         feats.append(ld.dcf_features(plan, td))
-        targets.append(torch.log(w))
+        targets.append(torch.log(w) + ld.target_offset(plan.lut, plan.W, 2))
         weights.append(ld.energy_weight(t, 2, recon, w, seed=50 + i))
     X = torch.cat(feats)
     Y = torch.cat(targets)
@@ -212,3 +212,10 @@ def test_gpu_learned_dcf_beats_plain_method():
         e_net, e_plain = _nrmse(img_net, img_pipe), _nrmse(img_plain, img_pipe)
         assert e_net < e_plain, (e_net, e_plain)
         assert e_net < 0.05, e_net
+
+
+def test_kernel_mass_of_a_flat_kernel():
+    from fastrecon_gb300 import learned_dcf as ld
+    flat = np.ones(512, np.float32)
+    assert abs(ld.kernel_mass(flat, 4.0, 2) - np.pi * 4.0) < 1e-6
+    assert abs(ld.kernel_mass(flat, 4.0, 3) - 4.0 / 3.0 * np.pi * 8.0) < 1e-6
