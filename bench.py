@@ -367,8 +367,8 @@ def run_ours(args, w):
         "data": "synthetic: seeded trajectory; exact k-space of a Gaussian-profile ellipsoid phantom x Gaussian "
                 "coil maps, 1% complex noise",
         "config": {"workload": w["desc"], "samples_per_coil": N, "coils": C, "grid": G,
-                   "l2": "inputs 1.9 GB per step exceed the 129 MB L2; no flush needed" if dim == 3 else
-                   "inputs smaller than L2; steps back to back",
+                   "l2": (f"inputs {N * (20 + 8 * C) / 1e9:.2f} GB per step exceed the 129 MB L2; no flush needed"
+                          if N * (20 + 8 * C) > 129e6 else "inputs smaller than the 129 MB L2; steps back to back"),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "recon_ms": ms,
         "stage_ms": stage_ms,

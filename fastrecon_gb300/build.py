@@ -81,6 +81,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
     build_cpp_api(force=force)
+    build_cli(force=force)
     return LIB
 
 
@@ -107,6 +108,29 @@ def build_cpp_api(force: bool = False) -> str:
         raise RuntimeError(f"C++ API build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, CPP_LIB)
     return CPP_LIB
+
+
+CLI_SRC = os.path.join(CPP_SRC, "cli", "fastrecon_main.cpp")
+CLI = os.path.join(LIBDIR, "fastrecon")
+
+
+def build_cli(force: bool = False) -> str:
+    """The reference's command-line program (Program/Main.cpp) on the C++ API:
+    fastrecon_gb300/_lib/fastrecon."""
+    hdrs = glob.glob(os.path.join(ROOT, "include", "fastrecon", "*.h"))
+    if not force and os.path.exists(CLI) and \
+            os.path.getmtime(CLI) >= max(os.path.getmtime(f) for f in hdrs + [CLI_SRC, CPP_LIB]):
+        return CLI
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-I",
+           os.path.join(CUDA_HOME, "include"), CLI_SRC, "-o", tmp, "-L", LIBDIR, "-lfastrecon", "-lfastrecon_gb300",
+           "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+           "-Wl,-rpath," + os.path.join(CUDA_HOME, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def clean():

@@ -168,6 +168,44 @@ __device__ float2 *line_fft(float2 *buf0, float2 *buf1, const FftPlan1D &pl, int
     return in;
 }
 
+// The same passes with the transform length, radices and buffer geometry
+// known at compile time (the index arithmetic becomes multiplies and
+// shifts).  The common grid sizes are instantiated; others use line_fft.
+template <int N, int R, int NS, int LINES, int LS, int ES>
+__device__ __forceinline__ void stockham_pass_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                 const float2 *__restrict__ tw)
+{
+    constexpr int M = N / R;
+    constexpr int TSTEP = N / (NS * R);  // r * k * TSTEP < N: no reduction needed
+    for (int idx = threadIdx.x; idx < M * LINES; idx += blockDim.x) {
+        const int l = idx / M, j = idx - l * M;
+        const int k = j % NS;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            float2 a = in[l * LS + (j + r * M) * ES];
+            if (r > 0 && k > 0) a = cmul(a, tw[r * k * TSTEP]);
+            v[r] = a;
+        }
+        dft<R>(v);
+        const int o = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[l * LS + (o + r * NS) * ES] = v[r];
+    }
+}
+
+template <int N, int NS, int LINES, int LS, int ES, int R, int... Rest>
+__device__ __forceinline__ float2 *fft_passes(float2 *in, float2 *out, const float2 *tw)
+{
+    stockham_pass_ct<N, R, NS, LINES, LS, ES>(in, out, tw);
+    __syncthreads();
+    if constexpr (sizeof...(Rest) == 0) {
+        return out;
+    } else {
+        return fft_passes<N, NS * R, LINES, LS, ES, Rest...>(out, in, tw);
+    }
+}
+
 // x stage: LINES consecutive lines of length n (contiguous) per CTA, keep
 // outputs [x0, x0 + rx).  in: nlines x n, out: nlines x rx.
 __global__ void __launch_bounds__(256) fft_x_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
@@ -260,6 +298,120 @@ __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__
             }
         }
     }
+}
+
+constexpr int kLinesX = 8;   // lines per CTA of the specialised x stage
+constexpr int kColsCt = 8;   // columns per CTA of the specialised column stages
+
+template <int N, int... Rs>
+__global__ void __launch_bounds__(256) fft_x_kernel_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                       long long nlines, int x0, int rx,
+                                                       const float2 *__restrict__ tw_g)
+{
+    extern __shared__ float2 sm[];
+    constexpr int LS = N + 1;
+    float2 *tw = sm;
+    float2 *b0 = tw + N;
+    float2 *b1 = b0 + kLinesX * LS;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
+    const long long l0 = (long long)blockIdx.x * kLinesX;
+    const int lines = (int)min((long long)kLinesX, nlines - l0);
+    for (int i = threadIdx.x; i < kLinesX * N; i += blockDim.x) {
+        const int l = i / N, e = i - l * N;
+        b0[l * LS + e] = l < lines ? in[(l0 + l) * N + e] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *res = fft_passes<N, 1, kLinesX, LS, 1, Rs...>(b0, b1, tw);
+    for (int i = threadIdx.x; i < lines * rx; i += blockDim.x) {
+        const int l = i / rx, e = i - l * rx;
+        out[(l0 + l) * rx + e] = res[l * LS + x0 + e];
+    }
+}
+
+template <int N, int... Rs>
+__global__ void __launch_bounds__(256) fft_col_kernel_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                         int y0, int ry, int ncols, long long stride,
+                                                         long long in_outer_stride, long long out_outer_stride,
+                                                         long long out_stride, const float2 *__restrict__ tw_g,
+                                                         int coils, long long cstride, float *__restrict__ sos_out,
+                                                         const float *__restrict__ deapod)
+{
+    extern __shared__ float2 sm[];
+    constexpr int C = kColsCt;
+    float2 *tw = sm;
+    float2 *b0 = tw + N;
+    float2 *b1 = b0 + N * C;
+    float *acc = reinterpret_cast<float *>(b1 + N * C);  // [ry][C] for the SoS stage
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
+    const int cblocks = (ncols + C - 1) / C;
+    const long long outer = blockIdx.x / cblocks;
+    const int c0 = (blockIdx.x % cblocks) * C;
+    const int cw = min(C, ncols - c0);
+    if (sos_out)
+        for (int i = threadIdx.x; i < ry * C; i += blockDim.x) acc[i] = 0.f;
+    for (int coil = 0; coil < (sos_out ? coils : 1); ++coil) {
+        const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < N * C; i += blockDim.x) {
+            const int e = i / C, c = i - e * C;
+            b0[i] = c < cw ? src[e * stride + c] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 *res = fft_passes<N, 1, C, 1, C, Rs...>(b0, b1, tw);
+        if (sos_out) {
+            for (int i = threadIdx.x; i < ry * C; i += blockDim.x) {
+                const int e = i / C, c = i - e * C;
+                const float2 v = res[(y0 + e) * C + c];
+                // x * conj(x) of the reference's SOS: re*re - im*(-im)
+                acc[i] = __fadd_rn(acc[i], __fsub_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, -v.y)));
+            }
+        } else {
+            float2 *dst = out + outer * out_outer_stride + c0;
+            for (int i = threadIdx.x; i < ry * C; i += blockDim.x) {
+                const int e = i / C, c = i - e * C;
+                if (c < cw) dst[e * out_stride + c] = res[(y0 + e) * C + c];
+            }
+        }
+    }
+    if (sos_out) {
+        __syncthreads();
+        float *dst = sos_out + outer * out_outer_stride + c0;
+        const float *dp = deapod ? deapod + outer * out_outer_stride + c0 : nullptr;
+        for (int i = threadIdx.x; i < ry * C; i += blockDim.x) {
+            const int e = i / C, c = i - e * C;
+            if (c < cw) {
+                float m = __fsqrt_rn(acc[i]);
+                if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                dst[e * out_stride + c] = m;
+            }
+        }
+    }
+}
+
+using FftXFn = void (*)(const float2 *, float2 *, long long, int, int, const float2 *);
+using FftColFn = void (*)(const float2 *, float2 *, int, int, int, long long, long long, long long, long long,
+                          const float2 *, int, long long, float *, const float *);
+struct CtKernels {
+    int n;
+    FftXFn x;
+    FftColFn col;
+};
+
+// Specialised sizes, radices in the order factor() chooses them.
+#define FR_CT(N, ...) {N, fft_x_kernel_ct<N, __VA_ARGS__>, fft_col_kernel_ct<N, __VA_ARGS__>}
+const CtKernels kCtKernels[] = {
+    FR_CT(64, 8, 8),          FR_CT(128, 8, 8, 2),      FR_CT(160, 8, 5, 4),     FR_CT(192, 8, 8, 3),
+    FR_CT(240, 8, 5, 3, 2),   FR_CT(256, 8, 8, 4),      FR_CT(320, 8, 8, 5),     FR_CT(384, 8, 8, 3, 2),
+    FR_CT(480, 8, 5, 4, 3),   FR_CT(512, 8, 8, 8),      FR_CT(640, 8, 8, 5, 2),  FR_CT(768, 8, 8, 4, 3),
+    FR_CT(1024, 8, 8, 8, 2),
+};
+#undef FR_CT
+
+const CtKernels *ct_kernels(int n)
+{
+    for (const CtKernels &k : kCtKernels)
+        if (k.n == n) return &k;
+    return nullptr;
 }
 
 bool factor(int n, FftPlan1D &pl)
@@ -359,9 +511,35 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
     const float2 *grid = reinterpret_cast<const float2 *>(d_grid);
     float2 *b1 = f->b1.as<float2>();
 
-    // x stage over all lines of all coils
     const long long Gz = f->dim == 3 ? G : 1;
     const long long nl = (long long)C * Gz * G;
+    if (const CtKernels *ck = ct_kernels(G)) {
+        // specialised sizes
+        const size_t smx = (size_t)(G + 2 * kLinesX * (G + 1)) * sizeof(float2);
+        if (smx > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(ck->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
+        ck->x<<<(unsigned)((nl + kLinesX - 1) / kLinesX), 256, smx, s>>>(grid, b1, nl, x0, rx, tw);
+        FR_CHECK_LAUNCH("fft_x_kernel_ct");
+        const size_t smc = (size_t)(G + 2 * G * kColsCt) * sizeof(float2) + (size_t)G * kColsCt * sizeof(float);
+        if (smc > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(ck->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+        const int cb = (rx + kColsCt - 1) / kColsCt;
+        if (f->dim == 2) {
+            ck->col<<<cb, 256, smc, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C, (long long)G * rx, d_out,
+                                         d_deapod);
+            FR_CHECK_LAUNCH("fft_col_kernel_ct(y, sos)");
+            return FR_OK;
+        }
+        float2 *b2 = f->b2.as<float2>();
+        ck->col<<<(unsigned)((long long)C * G * cb), 256, smc, s>>>(b1, b2, y0, ry, rx, rx, (long long)G * rx,
+                                                                   (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+        FR_CHECK_LAUNCH("fft_col_kernel_ct(y)");
+        ck->col<<<(unsigned)((long long)ry * cb), 256, smc, s>>>(b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx,
+                                                                (long long)ry * rx, tw, C, (long long)G * ry * rx,
+                                                                d_out, d_deapod);
+        FR_CHECK_LAUNCH("fft_col_kernel_ct(z, sos)");
+        return FR_OK;
+    }
+    // x stage over all lines of all coils
     const int L = f->lines_x;
     size_t smx = (size_t)(G + 2 * L * (G + 1)) * sizeof(float2);
     if (smx > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(fft_x_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));

@@ -360,7 +360,9 @@ def test_pils_ops_bit_exact(torch):
 # ------------------------------------------------------ pruned transform ----
 
 @pytest.mark.parametrize("dim,G,out", [(2, 64, (32, 32)), (2, 60, (40, 24)), (3, 30, (20, 20, 20)),
-                                       (3, 40, (24, 16, 10)), (3, 48, (48, 48, 48)), (2, 384, (256, 256))])
+                                       (3, 40, (24, 16, 10)), (3, 48, (48, 48, 48)), (2, 384, (256, 256)),
+                                       (3, 64, (40, 36, 32)), (2, 320, (256, 200)), (2, 160, (100, 100)),
+                                       (3, 128, (100, 100, 100))])
 def test_pruned_fft_crop_sos_matches_cufft(torch, dim, G, out):
     """fr_fft_crop_sos on a checkerboard-modulated grid == cuFFT + fftShift +
     crop + SoS of the same grid."""
