@@ -68,10 +68,8 @@ def parse():
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from fastrecon_gb300 import replicas
+    return replicas.env()
 
 
 def measured_peak():
@@ -299,10 +297,8 @@ def run_ours(args, w):
     elapsed = e0.elapsed_time(e1)  # ms
     scatter_ms, scatter_n = rec.profile_read()
     rec.profile(False)
-    if dist is not None:
-        t = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    from fastrecon_gb300 import replicas
+    elapsed = replicas.max_over_ranks(elapsed, dist, device=dev)  # replicas: the slowest rank's time
     ms = elapsed / args.steps
     value = ws * N * C * args.steps / (elapsed / 1e3) / 1e6
 
@@ -337,10 +333,7 @@ def run_ours(args, w):
         barrier()
         wall = time.perf_counter() - t0
         el2 = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([el2], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el2 = float(t.item())
+        el2 = replicas.max_over_ranks(el2, dist, device=dev)
         e2e = {"value": ws * N * C * k2 / (el2 / 1e3) / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": int(h_traj.numel() * 4 + h_dcf.numel() * 4 + h_kd.numel() * 8),
                "d2h_bytes_per_step": int(h_img.numel() * 4), "ms_per_step": el2 / k2,
@@ -394,7 +387,7 @@ def run_ours(args, w):
         import bench_extras
         del rec, traj, dcf, kd
         torch.cuda.empty_cache()
-        for key, fn in (("batched_spiral", bench_extras.batched_spiral),
+        for key, fn in (("radial2d", bench_extras.radial2d), ("batched_spiral", bench_extras.batched_spiral),
                         ("learned_dcf", bench_extras.learned_vs_pipe)):
             try:
                 line[key] = fn(torch)

@@ -10,7 +10,8 @@
   (320^3 grid), 256^3 SoS.  The same batch is reconstructed end to end by
   one captured graph with (a) the learned DCF (density features + network)
   and (b) the Pipe-Menon DCF (20 grid/degrid iterations), and the image
-  NRMSE of (a) against (b) is reported next to the time ratio.
+  NRMSE of (a) against (b) is reported next to the time ratio; (c) is the
+  learned DCF followed by 3 Pipe-Menon iterations started from it.
 
 Synthetic, seeded inputs stand in for scanner data (none ships with the
 reference): analytic k-space of a Gaussian-ellipsoid phantom times Gaussian
@@ -78,6 +79,24 @@ def batched_spiral(torch, steps=20, warmup=3, frames=64, coils=12, recon=192, os
                         "persistent launch per batch, replayed from a CUDA graph; tiling from the autotuner"}
 
 
+def radial2d(torch, steps=50, warmup=5):
+    """The reference's own CPU-runnable case, 2D radial (256 spokes x 512, 8
+    coils, |k| DCF, 512^2 grid, 256^2 SoS): the full recon step."""
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import synth
+    traj, dcf, kd = synth.make_case(**synth.CONFIGS["radial2d"], xp=torch, device="cuda")
+    traj = torch.from_numpy(traj).cuda()
+    dcf = torch.from_numpy(dcf).cuda()
+    n, c = traj.shape[0], kd.shape[0]
+    rec = fr.Recon(2, 256, 2.0, c, max_samples=n)
+    img = torch.empty(256 * 256, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream()
+    ms = _ms(torch, lambda: rec.run(traj, dcf, kd, out=img), steps, warmup, s)
+    return {"value": n * c / (ms / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_step": ms, "samples": n, "coils": c,
+            "workload": "2D radial: 256 uniformly spaced spokes x 512 samples, 8 coils, |k| DCF, KB width 4, "
+                        "os 2 -> 512^2 grid, 256^2 SoS (plan + grid + FFT + SoS per step)"}
+
+
 def _nrmse(torch, a, ref):
     a = a.double().flatten()
     ref = ref.double().flatten()
@@ -86,7 +105,7 @@ def _nrmse(torch, a, ref):
 
 
 def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os_=1.25, readout=256,
-                    spoke_range=(10_000, 60_000), seed=5, model=None):
+                    spoke_range=(10_000, 60_000), seed=5, model=None, refine=3):
     import fastrecon_gb300 as fr
     from fastrecon_gb300 import learned_dcf as ld
     from fastrecon_gb300 import synth
@@ -113,27 +132,30 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
     grid = torch.empty((coils, G ** 3), dtype=torch.complex64, device="cuda")
     out_size = (recon, recon, recon)
     fft = fr.FFT(3, (G, G, G), coils, +1)
-    img_l = torch.empty((volumes, recon ** 3), dtype=torch.float32, device="cuda")
-    img_p = torch.empty_like(img_l)
+    imgs = {m: torch.empty((volumes, recon ** 3), dtype=torch.float32, device="cuda")
+            for m in ("pipe", "learned", "learned_refined")}
     lib = fr.load()
 
     def run(mode, s):
         for i, V in enumerate(vols):
-            if mode == "learned":
+            if mode.startswith("learned"):
                 ld.density_counts(V["plan"], ld.RADII, stream=s, out=V["cnt"])
                 ld.dcf_features(V["plan"], V["traj"], counts=V["cnt"], stream=s, out=V["feat"])
                 net.forward(V["feat"], exp=True, scale=scale, out=V["w"], stream=s)
+                if mode == "learned_refined":
+                    fr.capi.check(lib.fr_dcf_pipe(V["plan"].h, refine, C.c_void_p(V["w"].data_ptr()),
+                                                  C.c_void_p(s.cuda_stream)), "fr_dcf_pipe")
             else:
                 V["w"].fill_(1.0)
                 fr.capi.check(lib.fr_dcf_pipe(V["plan"].h, 20, C.c_void_p(V["w"].data_ptr()),
                                               C.c_void_p(s.cuda_stream)), "fr_dcf_pipe")
             V["plan"].grid(V["kd"], V["w"], out=grid, stream=s)
             fft(grid, stream=s)  # the grid was flushed with the fftShift checkerboard
-            fr.sos(grid, 3, G, out_size, stream=s, out=(img_l if mode == "learned" else img_p)[i])
+            fr.sos(grid, 3, G, out_size, stream=s, out=imgs[mode][i])
 
     s = torch.cuda.Stream()
     res = {}
-    for mode in ("pipe", "learned"):
+    for mode in ("pipe", "learned", "learned_refined"):
         with torch.cuda.stream(s):
             run(mode, s)  # warm: buffers reach their size before capture
             s.synchronize()
@@ -143,10 +165,15 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
             ms = _ms(torch, g.replay, steps, warmup, s)
         res[mode] = ms
         del g
-    nr = [_nrmse(torch, img_l[i], img_p[i]) for i in range(volumes)]
+    nr = [_nrmse(torch, imgs["learned"][i], imgs["pipe"][i]) for i in range(volumes)]
+    nrr = [_nrmse(torch, imgs["learned_refined"][i], imgs["pipe"][i]) for i in range(volumes)]
     n = int(sum(V["n"] for V in vols))
     return {"learned_ms": res["learned"], "pipe_ms": res["pipe"], "speedup": res["pipe"] / res["learned"],
-            "nrmse_median": float(np.median(nr)), "nrmse_max": float(np.max(nr)), "volumes": volumes,
+            "nrmse_median": float(np.median(nr)), "nrmse_max": float(np.max(nr)),
+            "learned_refined": {"pipe_iterations": refine, "ms": res["learned_refined"],
+                                "speedup": res["pipe"] / res["learned_refined"],
+                                "nrmse_median": float(np.median(nrr)), "nrmse_max": float(np.max(nrr))},
+            "volumes": volumes,
             "samples": n, "coils": coils, "grid": G,
             "workload": f"{volumes} 3D kooshball volumes, seeded {spoke_range[0]}-{spoke_range[1]} golden-means "
                         f"spokes x {readout}, {coils} coils, os {os_} -> {G}^3 grid, {recon}^3 SoS; one captured "

@@ -171,6 +171,20 @@ __device__ float2 *line_fft(float2 *buf0, float2 *buf1, const FftPlan1D &pl, int
 // The same passes with the transform length, radices and buffer geometry
 // known at compile time (the index arithmetic becomes multiplies and
 // shifts).  The common grid sizes are instantiated; others use line_fft.
+// Element e of a line sits at e + e / 32 (one pad slot per 32) when the
+// elements are contiguous (ES == 1), which spreads the radix-strided writes
+// of a pass over the banks; column buffers (ES == lines) put the lines
+// fastest instead.
+template <int ES>
+__device__ __forceinline__ int pad_e(int e)
+{
+    if constexpr (ES == 1) {
+        return e + (e >> 5);
+    } else {
+        return e * ES;
+    }
+}
+
 template <int N, int R, int NS, int LINES, int LS, int ES>
 __device__ __forceinline__ void stockham_pass_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
                                                  const float2 *__restrict__ tw)
@@ -178,19 +192,22 @@ __device__ __forceinline__ void stockham_pass_ct(const float2 *__restrict__ in, 
     constexpr int M = N / R;
     constexpr int TSTEP = N / (NS * R);  // r * k * TSTEP < N: no reduction needed
     for (int idx = threadIdx.x; idx < M * LINES; idx += blockDim.x) {
-        const int l = idx / M, j = idx - l * M;
+        // contiguous lines: consecutive threads on consecutive butterflies;
+        // column buffers: consecutive threads on consecutive lines
+        const int l = ES == 1 ? idx / M : idx % LINES;
+        const int j = ES == 1 ? idx - l * M : idx / LINES;
         const int k = j % NS;
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            float2 a = in[l * LS + (j + r * M) * ES];
+            float2 a = in[l * LS + pad_e<ES>(j + r * M)];
             if (r > 0 && k > 0) a = cmul(a, tw[r * k * TSTEP]);
             v[r] = a;
         }
         dft<R>(v);
         const int o = (j / NS) * NS * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[l * LS + (o + r * NS) * ES] = v[r];
+        for (int r = 0; r < R; ++r) out[l * LS + pad_e<ES>(o + r * NS)] = v[r];
     }
 }
 
@@ -309,7 +326,7 @@ __global__ void __launch_bounds__(256) fft_x_kernel_ct(const float2 *__restrict_
                                                        const float2 *__restrict__ tw_g)
 {
     extern __shared__ float2 sm[];
-    constexpr int LS = N + 1;
+    constexpr int LS = N + N / 32 + 1;  // padded line (pad_e) + 1 against line-to-line conflicts
     float2 *tw = sm;
     float2 *b0 = tw + N;
     float2 *b1 = b0 + kLinesX * LS;
@@ -318,13 +335,13 @@ __global__ void __launch_bounds__(256) fft_x_kernel_ct(const float2 *__restrict_
     const int lines = (int)min((long long)kLinesX, nlines - l0);
     for (int i = threadIdx.x; i < kLinesX * N; i += blockDim.x) {
         const int l = i / N, e = i - l * N;
-        b0[l * LS + e] = l < lines ? in[(l0 + l) * N + e] : make_float2(0.f, 0.f);
+        b0[l * LS + pad_e<1>(e)] = l < lines ? in[(l0 + l) * N + e] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     float2 *res = fft_passes<N, 1, kLinesX, LS, 1, Rs...>(b0, b1, tw);
     for (int i = threadIdx.x; i < lines * rx; i += blockDim.x) {
         const int l = i / rx, e = i - l * rx;
-        out[(l0 + l) * rx + e] = res[l * LS + x0 + e];
+        out[(l0 + l) * rx + e] = res[l * LS + pad_e<1>(x0 + e)];
     }
 }
 
@@ -437,6 +454,9 @@ bool factor(int n, FftPlan1D &pl)
 }
 
 }  // namespace
+
+bool pruned_fft_specialised(int G) { return ct_kernels(G) != nullptr; }
+
 }  // namespace fr
 
 using namespace fr;
@@ -515,7 +535,7 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
     const long long nl = (long long)C * Gz * G;
     if (const CtKernels *ck = ct_kernels(G)) {
         // specialised sizes
-        const size_t smx = (size_t)(G + 2 * kLinesX * (G + 1)) * sizeof(float2);
+        const size_t smx = (size_t)(G + 2 * kLinesX * (G + G / 32 + 1)) * sizeof(float2);
         if (smx > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(ck->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
         ck->x<<<(unsigned)((nl + kLinesX - 1) / kLinesX), 256, smx, s>>>(grid, b1, nl, x0, rx, tw);
         FR_CHECK_LAUNCH("fft_x_kernel_ct");

@@ -246,6 +246,11 @@ int to_bf16_run(const float *d_a, void *d_b, int count, cudaStream_t s);
 }  // namespace fr
 
 namespace fr {
+// True when the pruned FFT has compile-time specialised passes for G.
+bool pruned_fft_specialised(int G);
+}  // namespace fr
+
+namespace fr {
 int deapod_seed_run(float *d_grid, int dim, int G, float hw, const float *d_lut, int L, int checkerboard,
                     cudaStream_t s);
 int deapod_map_run(const float *d_img, int dim, const unsigned *size, const unsigned *recon, float *d_out,

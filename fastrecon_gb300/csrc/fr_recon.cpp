@@ -32,8 +32,15 @@ struct fr_recon_s {
     bool timing = false;
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     float stage_ms[4] = {-1, -1, -1, -1};
+    // host-buffer runs: the k-space upload runs on its own stream while the
+    // trajectory is planned
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_start = nullptr, copy_done = nullptr;
     ~fr_recon_s()
     {
+        if (copy_start) cudaEventDestroy(copy_start);
+        if (copy_done) cudaEventDestroy(copy_done);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (plan) fr_plan_destroy(plan);
         if (fft) fr_fft_destroy(fft);
         if (fft1) fr_fft_destroy(fft1);
@@ -80,7 +87,10 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     }
     pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
     st = fr_plan_create(&pd, &r->plan);
-    if (!st && r->checkerboard && (d->flags & FR_RECON_PRUNED_FFT) && !(d->flags & FR_RECON_CUFFT)) {
+    // the pruned transform with fused crop + SoS where it is specialised for
+    // G (faster than cuFFT + SoS there), or when asked for
+    const bool want_pruned = (d->flags & FR_RECON_PRUNED_FFT) || pruned_fft_specialised((int)r->G);
+    if (!st && r->checkerboard && want_pruned && !(d->flags & FR_RECON_CUFFT)) {
         // the pruned transform where the grid size factors into 2, 3, 5
         if (fr_fft_crop_sos_create(d->dim, r->G, d->channels, r->d.out_size, &r->pruned) != FR_OK)
             r->pruned = nullptr;
@@ -129,12 +139,15 @@ static int ensure_deapod(fr_recon r, cudaStream_t s)
     return st;
 }
 
-int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata, size_t n,
-                 float *d_image, void *stream)
+}  // extern "C"
+
+namespace {
+// The recon of fr_recon_run; `kdata_ready` (if given) is waited for on the
+// stream between planning and gridding.
+int recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata, size_t n, float *d_image,
+              cudaStream_t s, cudaEvent_t kdata_ready)
 {
-    if (!r || !d_image || (n && (!d_traj || !d_dcf || !d_kdata)))
-        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
-    cudaStream_t s = (cudaStream_t)stream;
+    void *stream = (void *)s;
     int st = FR_OK;
     if (r->d.flags & FR_RECON_DEAPODIZE) {
         st = ensure_deapod(r, s);
@@ -145,6 +158,10 @@ int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const floa
     if (r->timing) cudaEventRecord(r->ev[0], s);
     st = fr_plan_set_trajectory(r->plan, d_traj, n, stream);
     if (r->timing) cudaEventRecord(r->ev[1], s);
+    if (!st && kdata_ready) {
+        cudaError_t e = cudaStreamWaitEvent(s, kdata_ready, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+    }
     if (!st) st = fr_grid(r->plan, d_kdata, d_dcf, r->d.channels, g, stream);
     if (r->timing) cudaEventRecord(r->ev[2], s);
     const float *deapod = (r->d.flags & FR_RECON_DEAPODIZE) ? r->deapod.as<float>() : nullptr;
@@ -167,6 +184,18 @@ int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const floa
     return st;
 }
 
+}  // namespace
+
+extern "C" {
+
+int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata, size_t n,
+                 float *d_image, void *stream)
+{
+    if (!r || !d_image || (n && (!d_traj || !d_dcf || !d_kdata)))
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return recon_run(r, d_traj, d_dcf, d_kdata, n, d_image, (cudaStream_t)stream, nullptr);
+}
+
 int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata, size_t n,
                       float *h_image, void *stream)
 {
@@ -179,13 +208,27 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
     if (r->h_traj.reserve(cap * 16) || r->h_dcf.reserve(cap * 4) ||
         r->h_kdata.reserve(cap * 8 * (size_t)r->d.channels) || r->h_img.reserve(nout * 4))
         return FR_ERR_OUT_OF_MEMORY;
+    if (!r->copy_stream) {
+        FR_CUDA(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));
+        FR_CUDA(cudaEventCreateWithFlags(&r->copy_start, cudaEventDisableTiming));
+        FR_CUDA(cudaEventCreateWithFlags(&r->copy_done, cudaEventDisableTiming));
+    }
+    cudaEvent_t ready = nullptr;
     if (n) {
+        // k-space on the copy stream (after whatever `s` has queued), the
+        // trajectory and DCF on `s`, which plans while the k-space arrives
+        FR_CUDA(cudaEventRecord(r->copy_start, s));
+        FR_CUDA(cudaStreamWaitEvent(r->copy_stream, r->copy_start, 0));
+        FR_CUDA(cudaMemcpyAsync(r->h_kdata.ptr, h_kdata, n * 8 * (size_t)r->d.channels, cudaMemcpyHostToDevice,
+                                r->copy_stream));
+        FR_CUDA(cudaEventRecord(r->copy_done, r->copy_stream));
+        ready = r->copy_done;
         FR_CUDA(cudaMemcpyAsync(r->h_traj.ptr, h_traj, n * 16, cudaMemcpyHostToDevice, s));
         FR_CUDA(cudaMemcpyAsync(r->h_dcf.ptr, h_dcf, n * 4, cudaMemcpyHostToDevice, s));
-        FR_CUDA(cudaMemcpyAsync(r->h_kdata.ptr, h_kdata, n * 8 * (size_t)r->d.channels, cudaMemcpyHostToDevice, s));
     }
-    int st = fr_recon_run(r, r->h_traj.as<float>(), r->h_dcf.as<float>(), r->h_kdata.as<float>(), n,
-                          r->h_img.as<float>(), stream);
+    int st = recon_run(r, r->h_traj.as<float>(), r->h_dcf.as<float>(), r->h_kdata.as<float>(), n,
+                       r->h_img.as<float>(), s, ready);
+    if (st && ready) cudaStreamSynchronize(r->copy_stream);  // leave no copy in flight on an error
     if (st) return st;
     FR_CUDA(cudaMemcpyAsync(h_image, r->h_img.ptr, nout * 4, cudaMemcpyDeviceToHost, s));
     FR_CUDA(cudaStreamSynchronize(s));

@@ -185,11 +185,17 @@ def target_offset(lut, kernel_width: float, dim: int) -> float:
     return 2.0 * float(np.log(kernel_mass(lut, kernel_width, dim)))
 
 
-def learned_dcf(plan: GridPlan, raw_traj, net: DCFNet, kmax: float = 0.0, stream=None):
-    """DCF of the plan's trajectory from the network."""
+def learned_dcf(plan: GridPlan, raw_traj, net: DCFNet, kmax: float = 0.0, refine: int = 0, stream=None):
+    """DCF of the plan's trajectory from the network; with refine > 0 the
+    network's weights start that many Pipe-Menon iterations (the iterated DCF
+    stays the reference: a few iterations from the learned start reach what
+    20 from uniform weights do)."""
     feats = dcf_features(plan, raw_traj, kmax=kmax, stream=stream)
     scale = float(np.exp(-target_offset(plan.lut, plan.W, plan.dim)))
-    return net.forward(feats, exp=True, scale=scale, stream=stream)
+    w = net.forward(feats, exp=True, scale=scale, stream=stream)
+    if refine > 0:
+        check(capi.load().fr_dcf_pipe(plan.h, int(refine), _ptr(w), C.c_void_p(_stream(stream))), "fr_dcf_pipe")
+    return w
 
 
 def train(net: DCFNet, features, log_target, weight=None, steps: int = 2000, batch: int = 16384, lr: float = 3e-3,

@@ -30,6 +30,7 @@ from . import synth
 HERE = os.path.dirname(os.path.abspath(__file__))
 MODELS = os.path.join(HERE, "models")
 PIPE_ITERS = 20
+REFINE = 3  # Pipe-Menon iterations started from the learned DCF
 
 
 def model_path(dim: int) -> str:
@@ -84,14 +85,16 @@ def evaluate(net, dim, trajs, coils=4, seed=100):
     for i, (t, recon, os_, fam) in enumerate(trajs):
         plan, td, w_pipe, x = pipe_and_features(t, dim, recon, os_)
         w_net = net.forward(x, exp=True, scale=math.exp(-ld.target_offset(plan.lut, plan.W, dim)))
+        w_ref = plan.dcf_pipe(REFINE, w0=w_net)
         w_plain = G_.dcf_analytic(td, dim, 1.0 if dim == 2 else 2.0)
         kd = synth.kspace(t, dim, recon, coils, seed=seed + i, xp=torch, device="cuda")
         rec = G_.Recon(dim, recon, os_, coils)
         img_pipe = rec.run(td, w_pipe, kd)
         e_net = nrmse(rec.run(td, w_net, kd), img_pipe)
+        e_ref = nrmse(rec.run(td, w_ref, kd), img_pipe)
         e_plain = nrmse(rec.run(td, w_plain, kd), img_pipe)
         out.append(dict(family=fam, samples=int(t.shape[0]), recon=recon, os=os_, nrmse_learned=e_net,
-                        nrmse_plain=e_plain))
+                        nrmse_learned_refined=e_ref, nrmse_plain=e_plain))
         del rec
     return out
 
@@ -148,6 +151,7 @@ def main(argv=None):
     rep = dict(dim=a.dim, trajectories=a.trajectories, samples=int(X.shape[0]), dataset_s=round(t_data, 1),
                train_s=round(t_train, 1), steps=a.steps, batch=a.batch, losses=losses,
                held_out=ev, median_nrmse_learned=float(np.median([e["nrmse_learned"] for e in ev])),
+               median_nrmse_learned_refined=float(np.median([e["nrmse_learned_refined"] for e in ev])),
                median_nrmse_plain=float(np.median([e["nrmse_plain"] for e in ev])), model=out)
     print(json.dumps(rep))
     return rep

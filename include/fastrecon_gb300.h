@@ -346,9 +346,11 @@ typedef struct fr_recon_s *fr_recon;
 
 enum {
     FR_RECON_DEAPODIZE = 1u << 0, /* divide by the kernel's image-domain apodization */
-    FR_RECON_CUFFT = 1u << 1,     /* the full cuFFT transform + crop/SoS kernel (the default) */
+    FR_RECON_CUFFT = 1u << 1,     /* always the full cuFFT transform + crop/SoS kernel */
     FR_RECON_PRUNED_FFT = 1u << 2 /* the pruned transform with fused crop + SoS (fr_fft_crop_sos)
-                                     where it applies (even G = 2^a 3^b 5^c <= 1024) */
+                                     wherever it applies (even G = 2^a 3^b 5^c <= 1024); by default
+                                     it is used for the grid sizes it has specialised passes for
+                                     (64, 128, 160, 192, 240, 256, 320, 384, 480, 512, 640, 768, 1024) */
 };
 
 typedef struct {

@@ -212,6 +212,12 @@ def test_gpu_learned_dcf_beats_plain_method():
         e_net, e_plain = _nrmse(img_net, img_pipe), _nrmse(img_plain, img_pipe)
         assert e_net < e_plain, (e_net, e_plain)
         assert e_net < 0.05, e_net
+        # three Pipe-Menon iterations from the learned start come close to twenty from ones
+        w_ref = ld.learned_dcf(plan, td, net, refine=3)
+        w3 = plan.dcf_pipe(3)
+        e_ref = _nrmse(rec.run(td, w_ref, kd).cpu().numpy(), img_pipe)
+        e3 = _nrmse(rec.run(td, w3, kd).cpu().numpy(), img_pipe)
+        assert e_ref < 0.02 and e_ref < e3, (e_ref, e3)
 
 
 def test_kernel_mass_of_a_flat_kernel():
