@@ -179,3 +179,62 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
                         f"spokes x {readout}, {coils} coils, os {os_} -> {G}^3 grid, {recon}^3 SoS; one captured "
                         "graph per DCF method (DCF + grid + FFT + crop/SoS for every volume)",
             "nrmse": "image NRMSE of the learned-DCF recon against the Pipe-DCF recon after the best scalar scale"}
+
+
+def exercise_kernels(torch):
+    """Every kernel family of the library once, on small inputs, between
+    cudaProfilerStart/Stop (for a per-kernel ncu capture with
+    --profile-from-start off): plan, scatter (single and persistent batch),
+    pruned FFT + SoS, cuFFT path + crop/SoS, analytic DCF, degridding,
+    Pipe-Menon, density features, the DCF network's forward/backward/Adam."""
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import batch as fb
+    from fastrecon_gb300 import learned_dcf as ld
+    from fastrecon_gb300 import synth
+    G, recon, coils = 192, 128, 16
+    t = synth.kooshball_3d(12500, 128)
+    td = torch.from_numpy(t).cuda()
+    kd = synth.kspace(t, 3, recon, coils, seed=1, xp=torch, device="cuda")
+    out3 = (recon, recon, recon)
+
+    def once():
+        dcf = fr.dcf_analytic(td, 3, 2.0)
+        plan = fr.GridPlan(3, G, 4.0, overgrid_factor=1.5, checkerboard=True)
+        plan.set_trajectory(td)
+        grid = plan.grid(kd, dcf)
+        fr.gridding.CropSoS(3, G, coils, out3)(grid)
+        plain = fr.GridPlan(3, G, 4.0, overgrid_factor=1.5)
+        plain.set_trajectory(td)
+        g2 = plain.grid(kd, dcf)
+        fr.FFT(3, (G, G, G), coils, +1)(g2)
+        fr.fft_shift(g2, 3, G)
+        fr.sos(g2, 3, G, out3)
+        plain.degrid(g2)
+        w = plain.dcf_pipe(2)
+        feats = ld.dcf_features(plain, td)
+        net = ld.DCFNet(seed=0)
+        net.forward(feats, exp=True)
+        net.loss_grad(feats[:65536], torch.log(w[:65536]))
+        net.adam()
+        counts = [4096, 20000, 9000]
+        bt = torch.from_numpy(np.concatenate([synth.spiral_2d(2, 2048), synth.spiral_2d(10, 2000),
+                                              synth.spiral_2d(5, 1800)])).cuda()
+        b = fb.GridBatch(2, 384, 4.0)
+        b.set_trajectories(bt, counts)
+        bk = torch.randn(sum(counts) * 12, dtype=torch.complex64, device="cuda")
+        b.grid(bk, fr.dcf_analytic(bt, 2, 1.0), 12)
+
+    once()  # warm: buffers, plans, attributes
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    once()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+
+
+if __name__ == "__main__":
+    import sys
+    import torch
+    if "--exercise" in sys.argv:
+        exercise_kernels(torch)
+        print("exercised")

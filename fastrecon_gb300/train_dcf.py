@@ -42,9 +42,12 @@ def draw_trajectory(dim: int, rng, n_min=10_000, n_max=2_000_000):
     n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
     os_ = float(rng.choice([1.25, 1.5, 2.0]))
     if dim == 3:
+        # matrix sizes independent of the readout, so that the sample density
+        # per grid cell spans sparse to dense (up to ~10 samples per cell)
         readout = int(rng.choice([64, 96, 128, 192, 256]))
+        recon = int(rng.choice([48, 64, 96, 128, 160, 192]))
         spokes = max(n // readout, 16)
-        return synth.kooshball_3d(spokes, readout), readout, os_, "koosh3d"
+        return synth.kooshball_3d(spokes, readout), recon, os_, "koosh3d"
     fam = rng.integers(0, 3)
     readout = int(rng.choice([128, 192, 256, 384, 512, 768, 1024]))
     spokes = max(n // readout, 8)
