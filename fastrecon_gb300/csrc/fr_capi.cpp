@@ -465,7 +465,8 @@ int fr_mlp_forward(const void *d_params, const float *d_features, size_t n, unsi
 {
     if (n && (!d_params || !d_features || !d_out)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
     if (reinterpret_cast<uintptr_t>(d_params) & 1) return fail(FR_ERR_INVALID_ARGUMENT, "parameters must be 2-byte aligned");
-    return mlp_forward_run(d_params, d_features, n, (flags & FR_MLP_EXP) ? 1 : 0, scale, d_out, (cudaStream_t)stream);
+    return mlp_forward_run(d_params, d_features, n, (flags & FR_MLP_EXP) ? 1 : 0, (flags & FR_MLP_RESIDUAL) ? 1 : 0,
+                           scale, d_out, (cudaStream_t)stream);
 }
 
 size_t fr_mlp_workspace_bytes(size_t n) { return mlp_workspace_bytes(n); }

@@ -12,8 +12,12 @@
 //            coils in coil order, sqrt (and / deapod)  -> [Rz][Ry][Rx]
 // (in 2D the y stage is the last one).  Each line is transformed in shared
 // memory by a self-sorting (Stockham) mixed-radix FFT with radix 2, 3, 4, 5
-// and 8 passes and a double-precision twiddle table rounded to float.
+// and 8 passes and a double-precision twiddle table rounded to float.  In 3D
+// at the specialised sizes the x stage is a batched 1D cuFFT into a full-size
+// buffer (faster than the shared-memory x stage there: every line is
+// transformed either way), and the y and z stages read its cropped columns.
 #include <cuda_runtime.h>
+#include <cufft.h>
 
 #include <cmath>
 #include <new>
@@ -317,11 +321,12 @@ __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__
     }
 }
 
-constexpr int kLinesX = 8;   // lines per CTA of the specialised x stage
+constexpr int kLinesX = 4;   // lines per CTA of the specialised x stage (128 threads)
+constexpr int kThreadsX = 128;
 constexpr int kColsCt = 8;   // columns per CTA of the specialised column stages
 
 template <int N, int... Rs>
-__global__ void __launch_bounds__(256) fft_x_kernel_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
+__global__ void __launch_bounds__(kThreadsX) fft_x_kernel_ct(const float2 *__restrict__ in, float2 *__restrict__ out,
                                                        long long nlines, int x0, int rx,
                                                        const float2 *__restrict__ tw_g)
 {
@@ -471,6 +476,12 @@ struct fr_fftcs_s {
     DevBuf b1;    // x-stage output
     DevBuf b2;    // y-stage output (3D)
     int lines_x = 8;
+    cufftHandle xplan = 0;  // 3D, specialised G: batched 1D x transforms
+    DevBuf bx;              // their output: channels x G^3 complex
+    ~fr_fftcs_s()
+    {
+        if (xplan) cufftDestroy(xplan);
+    }
 };
 
 extern "C" {
@@ -497,11 +508,24 @@ int fr_fft_crop_sos_create(int dim, unsigned G, int channels, const unsigned *ou
         tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
     const size_t Gz = dim == 3 ? G : 1;
+    const bool cufft_x = dim == 3 && ct_kernels((int)G) != nullptr;
     if (f->tw.reserve(G * sizeof(float2)) ||
-        f->b1.reserve((size_t)channels * Gz * G * f->out[0] * sizeof(float2)) ||
+        (!cufft_x && f->b1.reserve((size_t)channels * Gz * G * f->out[0] * sizeof(float2))) ||
+        (cufft_x && f->bx.reserve((size_t)channels * G * G * G * sizeof(float2))) ||
         (dim == 3 && f->b2.reserve((size_t)channels * G * f->out[1] * f->out[0] * sizeof(float2)))) {
         delete f;
         return FR_ERR_OUT_OF_MEMORY;
+    }
+    if (cufft_x) {
+        int nn[1] = {(int)G};
+        const long long lines = (long long)channels * G * G;
+        if (lines > 0x7FFFFFFFll ||
+            cufftPlanMany(&f->xplan, 1, nn, nullptr, 1, (int)G, nullptr, 1, (int)G, CUFFT_C2C, (int)lines) !=
+                CUFFT_SUCCESS) {
+            f->xplan = 0;
+            delete f;
+            return fail(FR_ERR_CUFFT, "cufftPlanMany (pruned FFT x stage)");
+        }
     }
     cudaError_t e = cudaMemcpy(f->tw.ptr, tw.data(), G * sizeof(float2), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -533,11 +557,34 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
 
     const long long Gz = f->dim == 3 ? G : 1;
     const long long nl = (long long)C * Gz * G;
+    if (const CtKernels *ck = ct_kernels(G); ck && f->xplan) {
+        // 3D, specialised size: x by cuFFT (out of place; C2C leaves its input
+        // intact), then the y and z stages on the cropped x columns
+        if (cufftSetStream(f->xplan, s) != CUFFT_SUCCESS ||
+            cufftExecC2C(f->xplan, (cufftComplex *)const_cast<float2 *>(grid), f->bx.as<cufftComplex>(),
+                         CUFFT_INVERSE) != CUFFT_SUCCESS)
+            return fail(FR_ERR_CUFFT, "cufftExecC2C (pruned FFT x stage)");
+        const size_t smc = (size_t)(G + 2 * G * kColsCt) * sizeof(float2) + (size_t)G * kColsCt * sizeof(float);
+        if (smc > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(ck->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smc));
+        const int cb = (rx + kColsCt - 1) / kColsCt;
+        float2 *b2 = f->b2.as<float2>();
+        // y stage: input bx[c][z][y][x], columns x0..x0+rx, element (y) stride G
+        ck->col<<<(unsigned)((long long)C * G * cb), 256, smc, s>>>(f->bx.as<float2>() + x0, b2, y0, ry, rx, G,
+                                                                   (long long)G * G, (long long)ry * rx, rx, tw, 1, 0,
+                                                                   nullptr, nullptr);
+        FR_CHECK_LAUNCH("fft_col_kernel_ct(y)");
+        ck->col<<<(unsigned)((long long)ry * cb), 256, smc, s>>>(b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx,
+                                                                (long long)ry * rx, tw, C, (long long)G * ry * rx,
+                                                                d_out, d_deapod);
+        FR_CHECK_LAUNCH("fft_col_kernel_ct(z, sos)");
+        return FR_OK;
+    }
     if (const CtKernels *ck = ct_kernels(G)) {
         // specialised sizes
         const size_t smx = (size_t)(G + 2 * kLinesX * (G + G / 32 + 1)) * sizeof(float2);
         if (smx > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(ck->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx));
-        ck->x<<<(unsigned)((nl + kLinesX - 1) / kLinesX), 256, smx, s>>>(grid, b1, nl, x0, rx, tw);
+        ck->x<<<(unsigned)((nl + kLinesX - 1) / kLinesX), kThreadsX, smx, s>>>(grid, b1, nl, x0, rx, tw);
         FR_CHECK_LAUNCH("fft_x_kernel_ct");
         const size_t smc = (size_t)(G + 2 * G * kColsCt) * sizeof(float2) + (size_t)G * kColsCt * sizeof(float);
         if (smc > 48 * 1024)

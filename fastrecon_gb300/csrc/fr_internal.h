@@ -236,8 +236,8 @@ int density_counts_run(fr_plan p, const int *radii, int nradii, int *d_counts, c
 int dcf_features_run(const int *d_counts, const float *d_raw, size_t n, int dim, const int *radii, int nradii,
                      float kmax, float *d_feat, unsigned *d_scratch, cudaStream_t s);
 size_t mlp_workspace_bytes(size_t n);
-int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, float scale, float *d_y,
-                    cudaStream_t s);
+int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, int residual, float scale,
+                    float *d_y, cudaStream_t s);
 int mlp_backward_run(const void *d_params, const float *d_x, const float *d_t, const float *d_w, size_t n, void *ws,
                      float *d_grad, float *d_loss, cudaStream_t s);
 int mlp_adam_run(float *d_master, void *d_params, const float *d_grad, float *d_m, float *d_v, int count, float lr,

@@ -113,7 +113,7 @@ __device__ __forceinline__ float forward_sample(const float *ps, const float *xs
 
 __global__ void __launch_bounds__(kFwdThreads) mlp_forward_kernel(const __nv_bfloat16 *__restrict__ pb,
                                                                   const float *__restrict__ x, long long n, int exp_out,
-                                                                  float scale, float *__restrict__ y)
+                                                                  int residual, float scale, float *__restrict__ y)
 {
     __shared__ __align__(16) float ps[NP + 3];
     load_params(pb, ps);
@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kFwdThreads) mlp_forward_kernel(const __nv_bfl
         float xs[NI], h2[NH];
 #pragma unroll
         for (int k = 0; k < NI; ++k) xs[k] = x[s * NI + k];
-        const float out = forward_sample(ps, xs, h2);
+        float out = forward_sample(ps, xs, h2);
+        if (residual) out = __fsub_rn(out, xs[1]);  // the network predicts log-DCF + log density (radius 2)
         y[s] = exp_out ? __fmul_rn(scale, expf(out)) : out;
     }
 }
@@ -312,14 +313,14 @@ size_t mlp_workspace_bytes(size_t n)
     return a + std::max<size_t>(gblocks, 1) * NP * 4 + (size_t)train_blocks((long long)std::max<size_t>(n, 1)) * 4 + 256;
 }
 
-int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, float scale, float *d_y,
-                    cudaStream_t s)
+int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_out, int residual, float scale,
+                    float *d_y, cudaStream_t s)
 {
     if (n == 0) return FR_OK;
     const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)n + kFwdThreads - 1) / kFwdThreads,
                                                                        (long long)sm_count_mlp() * 16));
     mlp_forward_kernel<<<blocks, kFwdThreads, 0, s>>>(static_cast<const __nv_bfloat16 *>(d_params), d_x, (long long)n,
-                                                      exp_out, scale, d_y);
+                                                      exp_out, residual, scale, d_y);
     FR_CHECK_LAUNCH("mlp_forward_kernel");
     return FR_OK;
 }

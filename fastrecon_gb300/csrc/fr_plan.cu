@@ -75,7 +75,22 @@ __global__ void bounds_kernel(const float4 *__restrict__ traj, size_t n, int dim
             hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
         }
     }
-    if ((threadIdx.x & 31) == 0) {
+    // one set of global atomics per block (few blocks: contention on the six
+    // words stays low)
+    __shared__ int wlo[32][3], whi[32][3];
+    const int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; ++d) {
+            wlo[warp][d] = lo[d];
+            whi[warp][d] = hi[d];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = min(lo[d], wlo[w][d]);
+                hi[d] = max(hi[d], whi[w][d]);
+            }
         for (int d = 0; d < dim; ++d) {
             if (lo[d] != INT_MAX) atomicMin(&b[kRawLoEnc + d], lo[d]);
             if (hi[d] != INT_MIN) atomicMax(&b[kRawHiEnc + d], hi[d]);
@@ -462,7 +477,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     FR_CHECK_LAUNCH("bounds_init_kernel");
     const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
     if (n > 0) {
-        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, p->dim, b);
+        bounds_kernel<<<std::min(grid_blocks(n, 256), 152 * 4), 256, 0, s>>>(raw, n, p->dim, b);
         FR_CHECK_LAUNCH("bounds_kernel");
     }
     scale_kernel<<<1, 1, 0, s>>>(b, p->dim, p->G);
@@ -564,7 +579,7 @@ int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_o
     FR_CHECK_LAUNCH("bounds_init_kernel");
     const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
     if (n > 0) {
-        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, dim, b);
+        bounds_kernel<<<std::min(grid_blocks(n, 256), 152 * 4), 256, 0, s>>>(raw, n, dim, b);
         FR_CHECK_LAUNCH("bounds_kernel");
     }
     scale_kernel<<<1, 1, 0, s>>>(b, dim, G);
@@ -599,7 +614,7 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
     FR_CHECK_LAUNCH("bounds_init_kernel");
     const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
     if (n > 0) {
-        bounds_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, pi.dim, b);
+        bounds_kernel<<<std::min(grid_blocks(n, 256), 152 * 4), 256, 0, s>>>(raw, n, pi.dim, b);
         FR_CHECK_LAUNCH("bounds_kernel");
     }
     scale_kernel<<<1, 1, 0, s>>>(b, pi.dim, pi.G);

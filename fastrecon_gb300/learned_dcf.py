@@ -35,6 +35,7 @@ OFF_B2 = OFF_W2 + HIDDEN * HIDDEN
 OFF_W3 = OFF_B2 + HIDDEN
 OFF_B3 = OFF_W3 + HIDDEN
 FR_MLP_EXP = 1
+FR_MLP_RESIDUAL = 2
 
 
 def _radii_arg(radii):
@@ -69,9 +70,12 @@ def dcf_features(plan: GridPlan, raw_traj, counts=None, radii=RADII, kmax: float
 class DCFNet:
     """The network's parameters (FP32 master + BF16 copy) and Adam state on the device."""
 
-    def __init__(self, params=None, seed: int = 0):
+    def __init__(self, params=None, seed: int = 0, residual: bool = False):
         torch = _torch()
         self.lib = capi.load()
+        # residual: the network is trained on log-DCF + feature 1 (log density
+        # at radius 2), so that its output is nearly density-independent
+        self.residual = bool(residual)
         if params is None:
             params = self.init_params(seed)
         self.master = torch.as_tensor(np.asarray(params, np.float32)).cuda().contiguous()
@@ -106,7 +110,8 @@ class DCFNet:
         n = features.shape[0]
         if out is None:
             out = torch.empty(n, dtype=torch.float32, device="cuda")
-        check(self.lib.fr_mlp_forward(_ptr(self.bf16), _ptr(features), n, FR_MLP_EXP if exp else 0, float(scale),
+        flags = (FR_MLP_EXP if exp else 0) | (FR_MLP_RESIDUAL if self.residual else 0)
+        check(self.lib.fr_mlp_forward(_ptr(self.bf16), _ptr(features), n, flags, float(scale),
                                       _ptr(out), C.c_void_p(_stream(stream))), "fr_mlp_forward")
         return out
 
@@ -149,11 +154,12 @@ class DCFNet:
         self.refresh()
 
     def save(self, path: str):
-        np.savez(path, params=self.master.cpu().numpy())
+        np.savez(path, params=self.master.cpu().numpy(), residual=np.int32(self.residual))
 
     @classmethod
     def load(cls, path: str):
-        return cls(np.load(path)["params"])
+        z = np.load(path)
+        return cls(z["params"], residual=bool(int(z["residual"])) if "residual" in z.files else False)
 
 
 def energy_weight(traj, dim, recon, w_pipe, seed=0, power=0.25):

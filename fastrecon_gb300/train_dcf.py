@@ -102,7 +102,7 @@ def evaluate(net, dim, trajs, coils=4, seed=100):
     return out
 
 
-def build_dataset(dim, n_traj, seed, per_traj=20000):
+def build_dataset(dim, n_traj, seed, per_traj=20000, residual=False):
     torch = G_._torch()
     rng = np.random.default_rng(seed)
     X, Y, C = [], [], []
@@ -115,7 +115,7 @@ def build_dataset(dim, n_traj, seed, per_traj=20000):
         n = t.shape[0]
         idx = torch.randint(0, n, (min(per_traj, n),), device="cuda", generator=g)
         X.append(x[idx])
-        Y.append(torch.log(w[idx]) + ld.target_offset(plan.lut, plan.W, dim))
+        Y.append(torch.log(w[idx]) + ld.target_offset(plan.lut, plan.W, dim) + (x[idx, 1] if residual else 0))
         C.append(c[idx])
     return torch.cat(X), torch.cat(Y), torch.cat(C)
 
@@ -131,14 +131,16 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--max-samples", type=int, default=2_000_000)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--residual", action="store_true",
+                    help="train on log-DCF + log density (radius 2): nearly density-independent targets")
     a = ap.parse_args(argv)
     torch = G_._torch()
     t0 = time.time()
-    X, Y, Cw = build_dataset(a.dim, a.trajectories, a.seed)
+    X, Y, Cw = build_dataset(a.dim, a.trajectories, a.seed, residual=a.residual)
     torch.cuda.synchronize()
     t_data = time.time() - t0
     mean, std = X.mean(0), X.std(0) + 1e-6
-    net = ld.DCFNet(seed=a.seed)
+    net = ld.DCFNet(seed=a.seed, residual=a.residual)
     t1 = time.time()
     losses = ld.train(net, (X - mean) / std, Y, Cw, steps=a.steps, batch=a.batch, lr=a.lr, seed=a.seed,
                       log_every=max(a.steps // 10, 1))
@@ -151,7 +153,7 @@ def main(argv=None):
     out = a.out or model_path(a.dim)
     os.makedirs(os.path.dirname(out), exist_ok=True)
     net.save(out)
-    rep = dict(dim=a.dim, trajectories=a.trajectories, samples=int(X.shape[0]), dataset_s=round(t_data, 1),
+    rep = dict(dim=a.dim, residual=a.residual, trajectories=a.trajectories, samples=int(X.shape[0]), dataset_s=round(t_data, 1),
                train_s=round(t_train, 1), steps=a.steps, batch=a.batch, losses=losses,
                held_out=ev, median_nrmse_learned=float(np.median([e["nrmse_learned"] for e in ev])),
                median_nrmse_learned_refined=float(np.median([e["nrmse_learned_refined"] for e in ev])),

@@ -264,7 +264,9 @@ int fr_dcf_features(fr_plan plan, const int *d_counts, const float *d_raw_traj, 
 #define FR_MLP_IN 5
 #define FR_MLP_HIDDEN 64
 #define FR_MLP_PARAMS (64 * 5 + 64 + 64 * 64 + 64 + 64 + 1)
-#define FR_MLP_EXP 1u /* write scale * exp(output): the DCF instead of its log */
+#define FR_MLP_EXP 1u      /* write scale * exp(output): the DCF instead of its log */
+#define FR_MLP_RESIDUAL 2u /* the network predicts log-DCF + feature 1 (log density at radius 2):
+                              subtract that feature from its output */
 int fr_mlp_forward(const void *d_params_bf16, const float *d_features, size_t n, unsigned flags, float scale,
                    float *d_out, void *stream);
 /* Workspace (16-byte aligned) for fr_mlp_backward on a batch of n samples. */

@@ -164,6 +164,8 @@ void orc_dcf_features(const int *counts, const float *raw_traj, size_t n, int di
 #define ORC_MLP_HIDDEN 64
 #define ORC_MLP_PARAMS (64 * 5 + 64 + 64 * 64 + 64 + 64 + 1)
 void orc_mlp_forward(const float *params, const float *x, size_t n, double *y);
+/* The same minus feature 1 (a network trained on log-DCF + log density). */
+void orc_mlp_forward_residual(const float *params, const float *x, size_t n, double *y);
 /* Weighted mean squared error (1/n) sum c_s (y_s - t_s)^2 (weight NULL: c = 1)
  * and its gradient (ORC_MLP_PARAMS doubles). */
 double orc_mlp_backward(const float *params, const float *x, const float *target, const float *weight, size_t n,

@@ -229,6 +229,12 @@ void orc_mlp_forward(const float *params, const float *x, size_t n, double *y)
     for (size_t s = 0; s < n; ++s) y[s] = forward1(params, x + s * NI, h1, h2);
 }
 
+void orc_mlp_forward_residual(const float *params, const float *x, size_t n, double *y)
+{
+    double h1[NH], h2[NH];
+    for (size_t s = 0; s < n; ++s) y[s] = forward1(params, x + s * NI, h1, h2) - (double)x[s * NI + 1];
+}
+
 double orc_mlp_backward(const float *params, const float *x, const float *target, const float *weight, size_t n,
                         double *grad)
 {

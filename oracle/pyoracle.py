@@ -209,6 +209,7 @@ class Oracle:
         lib.orc_density_counts.argtypes = [_f32p, C.c_size_t, C.c_int, C.c_uint, _i32p, C.c_int, _i32p]
         lib.orc_dcf_features.argtypes = [_i32p, _f32p, C.c_size_t, C.c_int, _i32p, C.c_int, C.c_float, _f32p]
         lib.orc_mlp_forward.argtypes = [_f32p, _f32p, C.c_size_t, _f64p]
+        lib.orc_mlp_forward_residual.argtypes = [_f32p, _f32p, C.c_size_t, _f64p]
         lib.orc_mlp_backward.argtypes = [_f32p, _f32p, _f32p, C.c_void_p, C.c_size_t, _f64p]
         lib.orc_mlp_backward.restype = C.c_double
         self._ext = True
@@ -258,10 +259,11 @@ class Oracle:
                                           float(kmax), out)
         return out
 
-    def mlp_forward(self, params, x):
+    def mlp_forward(self, params, x, residual=False):
         x = np.ascontiguousarray(x, np.float32)
         out = np.zeros(x.shape[0], np.float64)
-        self._ext_sigs().orc_mlp_forward(np.ascontiguousarray(params, np.float32), x, x.shape[0], out)
+        fn = self._ext_sigs().orc_mlp_forward_residual if residual else self._ext_sigs().orc_mlp_forward
+        fn(np.ascontiguousarray(params, np.float32), x, x.shape[0], out)
         return out
 
     def mlp_backward(self, params, x, target, weight=None):

@@ -116,6 +116,10 @@ def test_gpu_mlp_forward_matches_oracle(oracle):
     assert np.linalg.norm(got - want) <= TOL_FWD * np.linalg.norm(want)
     gexp = net.forward(torch.from_numpy(x).cuda(), exp=True, scale=0.25).cpu().numpy()
     assert np.allclose(gexp, 0.25 * np.exp(want), rtol=1e-4)
+    net.residual = True
+    got_r = net.forward(torch.from_numpy(x).cuda()).cpu().numpy()
+    want_r = oracle.mlp_forward(pf, x, residual=True)
+    assert np.linalg.norm(got_r - want_r) <= TOL_FWD * np.linalg.norm(want_r)
 
 
 @pytest.mark.gpu
