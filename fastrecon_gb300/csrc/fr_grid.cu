@@ -84,7 +84,7 @@ __device__ __forceinline__ void red_add_fx(unsigned a, float w, float vs)
     // 1.5 * 2^23 in the same fused operation lands in [2^23, 2^24), where the
     // float spacing is 1, and the low mantissa bits are the integer.
     const int i = __float_as_int(fmaf(w, vs, 12582912.f)) - 0x4B400000;
-    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(i) : "memory");
+    asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(a), "r"(i));
 }
 __device__ __forceinline__ int2 lds_i32x2(unsigned a)
 {
@@ -399,7 +399,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
                     const float4 en = lds_f32x4(lutE + 16u * (unsigned)k0);
                     const float w = s2 >= en.x ? en.z : en.y;
                     const int cell = (lz * Ty + ly) * Tx + lx;
-                    e = make_int2((cell * R + swz<R>(cell)) << 2, __float_as_int(w));
+                    e = make_int2((int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2)), __float_as_int(w));
                 }
             }
             const unsigned m = __ballot_sync(0xffffffffu, ok);
@@ -408,31 +408,35 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             buf ^= 1;
             if (ok) sts_s32x2(lst + 8u * __popc(m & lt), e);
             __syncwarp();
+            // Entries hold the shared address of the tap's cell row; the tile
+            // is 128-byte aligned, so the lane's swizzled float is address ^
+            // f0b.  Lanes of coils beyond the last carry value 0 and add 0.
             const int n = __popc(m);
             if (NG == 1) {
                 int k = 0;
-                for (; k + 1 < n; k += 2) {
+                for (; k + 3 < n; k += 4) {
                     const int4 e2 = lds_s32x4(lst + 8u * k);
-                    const unsigned a0 = acc + ((unsigned)e2.x ^ f0b), a1 = acc + ((unsigned)e2.z ^ f0b);
+                    const int4 e3 = lds_s32x4(lst + 8u * k + 16u);
+                    const unsigned a0 = (unsigned)e2.x ^ f0b, a1 = (unsigned)e2.z ^ f0b;
+                    const unsigned a2 = (unsigned)e3.x ^ f0b, a3 = (unsigned)e3.z ^ f0b;
 #pragma unroll
                     for (int kk = 0; kk < NF; ++kk) {
-                        if (coil_ok[kk]) {
-                            red_add_fx(a0 + 128u * kk, __int_as_float(e2.y), val[kk]);
-                            red_add_fx(a1 + 128u * kk, __int_as_float(e2.w), val[kk]);
-                        }
+                        red_add_fx(a0 + 128u * kk, __int_as_float(e2.y), val[kk]);
+                        red_add_fx(a1 + 128u * kk, __int_as_float(e2.w), val[kk]);
+                        red_add_fx(a2 + 128u * kk, __int_as_float(e3.y), val[kk]);
+                        red_add_fx(a3 + 128u * kk, __int_as_float(e3.w), val[kk]);
                     }
                 }
-                if (k < n) {
+                for (; k < n; ++k) {
                     const int2 e1 = lds_s32x2(lst + 8u * k);
-                    const unsigned a0 = acc + ((unsigned)e1.x ^ f0b);
+                    const unsigned a0 = (unsigned)e1.x ^ f0b;
 #pragma unroll
-                    for (int kk = 0; kk < NF; ++kk)
-                        if (coil_ok[kk]) red_add_fx(a0 + 128u * kk, __int_as_float(e1.y), val[kk]);
+                    for (int kk = 0; kk < NF; ++kk) red_add_fx(a0 + 128u * kk, __int_as_float(e1.y), val[kk]);
                 }
             } else {
                 for (int k = q; k < n; k += NG) {
                     const int2 e1 = lds_s32x2(lst + 8u * k);
-                    if (coil_ok[0]) red_add_fx(acc + ((unsigned)e1.x ^ f0b), __int_as_float(e1.y), val[0]);
+                    red_add_fx((unsigned)e1.x ^ f0b, __int_as_float(e1.y), val[0]);
                 }
             }
         }
@@ -456,10 +460,20 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
 }
 
 // One CTA per (work item, coil group).
+// The dynamic shared memory from its first 128-byte boundary (every launch
+// adds 128 bytes): tap-list entries carry absolute tile-row addresses that a
+// lane XORs with its float offset.
+__device__ __forceinline__ float4 *aligned_smem(float4 *raw)
+{
+    const unsigned a = smem_addr(raw);
+    return raw + (((128u - (a & 127u)) & 127u) >> 4);
+}
+
 template <int DIM, int R>
 __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
 {
-    extern __shared__ float4 smem4[];
+    extern __shared__ float4 smem_raw[];
+    float4 *smem4 = aligned_smem(smem_raw);
     const WorkItem it = P.items[blockIdx.x];
     if (it.count > 0) {
         stage_tables<R>(P, smem4);
@@ -475,7 +489,8 @@ __global__ void __launch_bounds__(512) grid_tiles_kernel(GridParams P)
 template <int DIM, int R>
 __global__ void __launch_bounds__(512) grid_persistent_kernel(GridParams P)
 {
-    extern __shared__ float4 smem4[];
+    extern __shared__ float4 smem_raw[];
+    float4 *smem4 = aligned_smem(smem_raw);
     __shared__ long long next;
     stage_tables<R>(P, smem4);
     const long long nitems = P.nwork / P.ngroups;
@@ -571,8 +586,9 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
 
 size_t grid_smem_bytes(long long K, int R, int L)
 {
-    // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode table
-    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64 + 3 * 64 * 4;
+    // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode
+    // table + scale words + alignment of the tile to 128 bytes
+    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64 + 3 * 64 * 4 + 128;
 }
 
 int floats_per_cell(int coil_group)
