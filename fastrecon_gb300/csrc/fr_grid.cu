@@ -210,6 +210,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
 
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
+constexpr int kScaleBatch = 4;     // records per warp step of the scale pass
 
 // Shared-memory layout of the scatter: accumulator tile [K][R] int32 | LUT
 // entries [L] float4 | per warp two tap-list buffers [32] {byte offset of the
@@ -305,17 +306,38 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         float bs[NF], bm[NF];
 #pragma unroll
         for (int k = 0; k < NF; ++k) bs[k] = bm[k] = 0.f;
-        for (int j = warp; j < it.count; j += kWarps) {
-            const unsigned long long rec = recs[j];
-            const unsigned box = (unsigned)(rec >> 32);
-            if (((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) == 0) continue;
-            const unsigned s = (unsigned)rec;
-            const float d = dcf[s];
+        // kScaleBatch records per warp step, every load of the step issued
+        // before the first is used (the pass is bound by the latency of these
+        // gathers); lane b of the step also pulls record b's position into L1
+        // for the accumulation pass.
+        for (int j0 = warp * kScaleBatch; j0 < it.count; j0 += kWarps * kScaleBatch) {
+            unsigned sl = 0u;
+            bool vl = false;
+            if (lane < kScaleBatch && j0 + lane < it.count) {
+                const unsigned long long rec = recs[j0 + lane];
+                const unsigned box = (unsigned)(rec >> 32);
+                sl = (unsigned)rec;
+                vl = ((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) != 0;
+                if (vl) asm volatile("prefetch.global.L1 [%0];" ::"l"(traj + sl));
+            }
+            const unsigned vm = __ballot_sync(0xffffffffu, vl);
+            float db[kScaleBatch], kb[kScaleBatch][NF];
 #pragma unroll
-            for (int k = 0; k < NF; ++k) {
-                const float a = coil_ok[k] ? fabsf(__fmul_rn(d, kdf[k][2 * (size_t)s])) : 0.f;
-                bs[k] += a;
-                bm[k] = fmaxf(bm[k], a);
+            for (int b = 0; b < kScaleBatch; ++b) {
+                const unsigned sv = __shfl_sync(0xffffffffu, sl, b);
+                const bool v = (vm >> b) & 1u;
+                db[b] = v ? dcf[sv] : 0.f;
+#pragma unroll
+                for (int k = 0; k < NF; ++k) kb[b][k] = v && coil_ok[k] ? kdf[k][2 * (size_t)sv] : 0.f;
+            }
+#pragma unroll
+            for (int b = 0; b < kScaleBatch; ++b) {
+#pragma unroll
+                for (int k = 0; k < NF; ++k) {
+                    const float a = fabsf(__fmul_rn(db[b], kb[b][k]));
+                    bs[k] += a;
+                    bm[k] = fmaxf(bm[k], a);
+                }
             }
         }
         if (q == 0) {
