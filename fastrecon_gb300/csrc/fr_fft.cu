@@ -20,6 +20,7 @@
 #include <cufft.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <new>
 #include <vector>
 
@@ -119,6 +120,8 @@ __device__ __forceinline__ void dft(float2 *v)
     if constexpr (R == 5) dft5(v);
     if constexpr (R == 8) dft8(v);
 }
+
+#include "fr_fft_reg.cuh"
 
 // One Stockham pass of radix R over `lines` lines in shared memory:
 // for j < n/R: v[r] = in[j + r n/R] * W^(r (j mod ns) n/(ns R)), DFT_R,
@@ -436,6 +439,30 @@ const CtKernels *ct_kernels(int n)
     return nullptr;
 }
 
+// Register two-step stages (fr_fft_reg.cuh) for the specialised sizes.
+struct RegKernels {
+    int n;
+    FftXFn x;
+    FftColFn col, col_sos;
+    size_t xsmem, colsmem;
+    int xthreads, colthreads;
+};
+#define FR_REG(N)                                                                                            \
+    {N, fft_x_kernel_reg<N>, fft_col_kernel_reg<N, false>, fft_col_kernel_reg<N, true>, reg_x_smem<N>(),      \
+     reg_col_smem<N>(), kRegLinesX * RegSplit<N>::TH, kRegCols * RegSplit<N>::TH}
+const RegKernels kRegKernels[] = {
+    FR_REG(64),  FR_REG(128), FR_REG(160), FR_REG(192), FR_REG(240), FR_REG(256), FR_REG(320),
+    FR_REG(384), FR_REG(480), FR_REG(512), FR_REG(640),
+};
+#undef FR_REG
+
+const RegKernels *reg_kernels(int n)
+{
+    for (const RegKernels &k : kRegKernels)
+        if (k.n == n) return &k;
+    return nullptr;
+}
+
 bool factor(int n, FftPlan1D &pl)
 {
     pl.n = n;
@@ -476,7 +503,8 @@ struct fr_fftcs_s {
     DevBuf b1;    // x-stage output
     DevBuf b2;    // y-stage output (3D)
     int lines_x = 8;
-    cufftHandle xplan = 0;  // 3D, specialised G: batched 1D x transforms
+    const RegKernels *reg = nullptr;  // register two-step stages for this G (else Stockham passes)
+    cufftHandle xplan = 0;  // 3D, specialised G without register stages: batched 1D x transforms
     DevBuf bx;              // their output: channels x G^3 complex
     ~fr_fftcs_s()
     {
@@ -508,7 +536,11 @@ int fr_fft_crop_sos_create(int dim, unsigned G, int channels, const unsigned *ou
         tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
     }
     const size_t Gz = dim == 3 ? G : 1;
-    const bool cufft_x = dim == 3 && ct_kernels((int)G) != nullptr;
+    {
+        const char *st = std::getenv("FR_FFT_STOCKHAM");
+        if (!(st && std::atoi(st) != 0)) f->reg = reg_kernels((int)G);
+    }
+    const bool cufft_x = dim == 3 && ct_kernels((int)G) != nullptr && !f->reg;
     if (f->tw.reserve(G * sizeof(float2)) ||
         (!cufft_x && f->b1.reserve((size_t)channels * Gz * G * f->out[0] * sizeof(float2))) ||
         (cufft_x && f->bx.reserve((size_t)channels * G * G * G * sizeof(float2))) ||
@@ -557,6 +589,33 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
 
     const long long Gz = f->dim == 3 ? G : 1;
     const long long nl = (long long)C * Gz * G;
+    if (const RegKernels *rk = f->reg) {
+        // register two-step stages: x (cropped), y (cropped), z or y with SoS
+        if (rk->xsmem > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(rk->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->xsmem));
+        if (rk->colsmem > 48 * 1024) {
+            FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
+            FR_CUDA(cudaFuncSetAttribute(rk->col_sos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
+        }
+        rk->x<<<(unsigned)((nl + kRegLinesX - 1) / kRegLinesX), rk->xthreads, rk->xsmem, s>>>(grid, b1, nl, x0, rx, tw);
+        FR_CHECK_LAUNCH("fft_x_kernel_reg");
+        const int cb = (rx + kRegCols - 1) / kRegCols;
+        if (f->dim == 2) {
+            rk->col_sos<<<cb, rk->colthreads, rk->colsmem, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C,
+                                                            (long long)G * rx, d_out, d_deapod);
+            FR_CHECK_LAUNCH("fft_col_kernel_reg(y, sos)");
+            return FR_OK;
+        }
+        float2 *b2 = f->b2.as<float2>();
+        rk->col<<<(unsigned)((long long)C * G * cb), rk->colthreads, rk->colsmem, s>>>(
+            b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+        FR_CHECK_LAUNCH("fft_col_kernel_reg(y)");
+        rk->col_sos<<<(unsigned)((long long)ry * cb), rk->colthreads, rk->colsmem, s>>>(
+            b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C, (long long)G * ry * rx, d_out,
+            d_deapod);
+        FR_CHECK_LAUNCH("fft_col_kernel_reg(z, sos)");
+        return FR_OK;
+    }
     if (const CtKernels *ck = ct_kernels(G); ck && f->xplan) {
         // 3D, specialised size: x by cuFFT (out of place; C2C leaves its input
         // intact), then the y and z stages on the cropped x columns

@@ -362,7 +362,10 @@ def test_pils_ops_bit_exact(torch):
 @pytest.mark.parametrize("dim,G,out", [(2, 64, (32, 32)), (2, 60, (40, 24)), (3, 30, (20, 20, 20)),
                                        (3, 40, (24, 16, 10)), (3, 48, (48, 48, 48)), (2, 384, (256, 256)),
                                        (3, 64, (40, 36, 32)), (2, 320, (256, 200)), (2, 160, (100, 100)),
-                                       (3, 128, (100, 100, 100))])
+                                       (3, 128, (100, 100, 100)), (2, 128, (64, 64)), (2, 192, (96, 160)),
+                                       (2, 240, (128, 128)), (2, 256, (200, 180)), (2, 480, (300, 300)),
+                                       (2, 512, (256, 256)), (2, 640, (400, 320)), (3, 160, (100, 80, 60)),
+                                       (3, 192, (128, 128, 128)), (3, 240, (160, 150, 140))])
 def test_pruned_fft_crop_sos_matches_cufft(torch, dim, G, out):
     """fr_fft_crop_sos on a checkerboard-modulated grid == cuFFT + fftShift +
     crop + SoS of the same grid."""
