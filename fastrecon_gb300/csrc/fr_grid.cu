@@ -120,12 +120,6 @@ __device__ __forceinline__ void sts_s32x2(unsigned a, int2 v)
 {
     asm volatile("st.shared.v2.s32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
 }
-__device__ __forceinline__ unsigned lds_u8(unsigned a)
-{
-    unsigned r;
-    asm volatile("ld.shared.u8 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
-    return r;
-}
 
 // Flush (or zero-fill) the tile's cells for one coil group.  Threads map to
 // (x pair, row): each writes two consecutive x cells as one 16-byte store
@@ -211,21 +205,34 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
 constexpr int kScaleBatch = 4;     // records per warp step of the scale pass
+constexpr int kDecBytes = 16 * 64 * 16;  // tap decode table: 16 box classes x 64 taps x float4
 
 // Shared-memory layout of the scatter: accumulator tile [K][R] int32 | LUT
-// entries [L] float4 | per warp two tap-list buffers [32] {byte offset of the
-// tap's cell row (swizzled), weight} | tap decode table [16][64] bytes |
+// entries [L] float4 | per warp two tap-list buffers [32] {shared address of
+// the tap's cell row (swizzled), weight} | tap decode table [16][64] float4 |
 // per coil float: bound sum, bound max, inverse scale [3][64] floats.
+//
+// Decode table: for a tap box of nx x ny x nz cells (nx, ny <= 4; class
+// (nx-1)*4 + (ny-1)), tap tt = ix + nx (iy + ny iz) is {ix, iy, iz, cell
+// offset (iz Ty + iy) Tx + ix} with the offsets as floats (exact) and the cell
+// offset as integer bits.  Built without divisions: t / n for n <= 4 and
+// t < 64 is (t * {128, 64, 43, 32}[n-1]) >> 7.
 template <int R>
 __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
 {
     float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)P.K * R);
-    unsigned char *dec_g = reinterpret_cast<unsigned char *>(lutE_g + P.L) + kWarps * 2 * kListEntries * 8;
+    float4 *dec_g = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(lutE_g + P.L) +
+                                               kWarps * 2 * kListEntries * 8);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutE_g[i] = P.lut_e[i];
+    const int Tx = P.tile[0], Ty = P.tile[1];
     for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
-        const int nx = (i >> 8) + 1, ny = ((i >> 6) & 3) + 1, tt = i & 63;
-        const int ix = tt % nx, iy = (tt / nx) % ny, iz = tt / (nx * ny);
-        dec_g[i] = (unsigned char)(ix | (iy << 2) | ((iz & 3) << 4));
+        const int c = i >> 6, tt = i & 63;
+        const int nx = (c >> 2) + 1, ny = (c & 3) + 1;
+        const int mx = nx == 1 ? 128 : nx == 2 ? 64 : nx == 3 ? 43 : 32;
+        const int my = ny == 1 ? 128 : ny == 2 ? 64 : ny == 3 ? 43 : 32;
+        const int q1 = (tt * mx) >> 7, ix = tt - q1 * nx;
+        const int iz = (q1 * my) >> 7, iy = q1 - iz * ny;
+        dec_g[i] = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
     }
 }
 
@@ -256,7 +263,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     const float *dcf = P.dcf + s_off;
 
     float *bsum_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + (size_t)K * R * 4 +
-                                              (size_t)P.L * 16 + kWarps * 2 * kListEntries * 8 + 16 * 64);
+                                              (size_t)P.L * 16 + kWarps * 2 * kListEntries * 8 + kDecBytes);
     unsigned *bmax_s = reinterpret_cast<unsigned *>(bsum_s + 64);
     float *inv_s = bsum_s + 128;
 
@@ -385,58 +392,52 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         for (int k = 0; k < NF; ++k)
             val[k] = coil_ok[k] ? __fmul_rn(__fmul_rn(d, kdf[k][2 * (size_t)s]), sc[k]) : 0.f;  // GridLut.cpp:109, scaled
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
-        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64);
+        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 16);
+        // box origin as floats (integers below 2^24: exact), its first cell
+        const float fgx = (float)(ox + lx0), fgy = (float)(oy + ly0), fgz = (float)(oz + lz0);
+        const int cell0 = (lz0 * Ty + ly0) * Tx + lx0;
         const int nround = (ntap + 31) >> 5;
         for (int rnd = 0; rnd < nround; ++rnd) {
+            // Every lane evaluates its tap (lanes past the box too, on table
+            // entries that exist) and the ballot keeps the valid ones.
             const int tt = rnd * 32 + lane;
-            bool ok = tt < ntap;
-            int ix = 0, iy = 0, iz = 0;
-            if (ok) {
-                if (small) {
-                    const unsigned code = lds_u8(dtab + tt);
-                    ix = code & 3;
-                    iy = (code >> 2) & 3;
-                    iz = code >> 4;
-                } else {
-                    ix = tt % nx;
-                    const int r = tt / nx;
-                    iy = r % ny;
-                    iz = r / ny;
-                }
+            float4 d4;
+            if (small) {  // warp-uniform; nround <= 2, so tt < 64
+                d4 = lds_f32x4(dtab + 16u * (unsigned)tt);
+            } else {
+                const int ix = tt % nx, r = tt / nx, iy = r % ny, iz = r / ny;
+                d4 = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
             }
-            int2 e = make_int2(0, 0);
-            if (ok) {
-                const int lx = lx0 + ix, ly = ly0 + iy, lz = lz0 + iz;
-                const float dx = __fsub_rn((float)(ox + lx), p.x);
-                const float dy = __fsub_rn((float)(oy + ly), p.y);
-                const float dz = DIM == 3 ? __fsub_rn((float)(oz + lz), p.z) : 0.f;
-                // GridLut.cpp:131: dk^2 = (dz^2 + dy^2) + dx^2, unfused
-                const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy)), __fmul_rn(dx, dx));
-                ok = s2 < P.smax;  // sqrtf(s2) < kHW
-                if (ok) {
-                    // first guess k0 in {ki-1, ki}, then one exact threshold test
-                    float a;
-                    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(s2));
-                    const int k0 = min((int)fmaf(a, P.kc, P.khalf), P.L - 1);
-                    const float4 en = lds_f32x4(lutE + 16u * (unsigned)k0);
-                    const float w = s2 >= en.x ? en.z : en.y;
-                    const int cell = (lz * Ty + ly) * Tx + lx;
-                    e = make_int2((int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2)), __float_as_int(w));
-                }
-            }
+            const float dx = __fsub_rn(__fadd_rn(fgx, d4.x), p.x);
+            const float dy = __fsub_rn(__fadd_rn(fgy, d4.y), p.y);
+            const float dz = DIM == 3 ? __fsub_rn(__fadd_rn(fgz, d4.z), p.z) : 0.f;
+            // GridLut.cpp:131: dk^2 = (dz^2 + dy^2) + dx^2, unfused
+            const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dz, dz), __fmul_rn(dy, dy)), __fmul_rn(dx, dx));
+            const bool ok = tt < ntap && s2 < P.smax;  // sqrtf(s2) < kHW
+            // first guess k0 in {ki-1, ki}, then one exact threshold test
+            float a;
+            asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(s2));
+            const int k0 = (int)fminf(fmaf(a, P.kc, P.khalf), (float)(P.L - 1));
+            const float4 en = lds_f32x4(lutE + 16u * (unsigned)k0);
+            const float w = s2 >= en.x ? en.z : en.y;
+            const int cell = cell0 + __float_as_int(d4.w);
+            const int ex = (int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2));
             const unsigned m = __ballot_sync(0xffffffffu, ok);
             if (m == 0) continue;
+            // the list, padded to a multiple of four with weight-0 copies of
+            // the first entry (they add exactly 0 to a cell of this sample)
+            const int n = __popc(m), n4 = (n + 3) & ~3;
+            const int e0x = __shfl_sync(0xffffffffu, ex, __ffs(m) - 1);
             const unsigned lst = mylist + buf * (kListEntries * 8);
             buf ^= 1;
-            if (ok) sts_s32x2(lst + 8u * __popc(m & lt), e);
+            const int pos = ok ? __popc(m & lt) : n + __popc(~m & lt);
+            if (pos < n4) sts_s32x2(lst + 8u * (unsigned)pos, ok ? make_int2(ex, __float_as_int(w)) : make_int2(e0x, 0));
             __syncwarp();
             // Entries hold the shared address of the tap's cell row; the tile
             // is 128-byte aligned, so the lane's swizzled float is address ^
             // f0b.  Lanes of coils beyond the last carry value 0 and add 0.
-            const int n = __popc(m);
             if (NG == 1) {
-                int k = 0;
-                for (; k + 3 < n; k += 4) {
+                for (int k = 0; k < n4; k += 4) {
                     const int4 e2 = lds_s32x4(lst + 8u * k);
                     const int4 e3 = lds_s32x4(lst + 8u * k + 16u);
                     const unsigned a0 = (unsigned)e2.x ^ f0b, a1 = (unsigned)e2.z ^ f0b;
@@ -449,14 +450,8 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
                         red_add_fx(a3 + 128u * kk, __int_as_float(e3.w), val[kk]);
                     }
                 }
-                for (; k < n; ++k) {
-                    const int2 e1 = lds_s32x2(lst + 8u * k);
-                    const unsigned a0 = (unsigned)e1.x ^ f0b;
-#pragma unroll
-                    for (int kk = 0; kk < NF; ++kk) red_add_fx(a0 + 128u * kk, __int_as_float(e1.y), val[kk]);
-                }
             } else {
-                for (int k = q; k < n; k += NG) {
+                for (int k = q; k < n4; k += NG) {
                     const int2 e1 = lds_s32x2(lst + 8u * k);
                     red_add_fx((unsigned)e1.x ^ f0b, __int_as_float(e1.y), val[0]);
                 }
@@ -610,7 +605,7 @@ size_t grid_smem_bytes(long long K, int R, int L)
 {
     // accumulator tile + LUT + double-buffered per-warp tap lists + tap decode
     // table + scale words + alignment of the tile to 128 bytes
-    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + 16 * 64 + 3 * 64 * 4 + 128;
+    return (size_t)K * R * 4 + (size_t)L * 16 + (size_t)kWarps * 2 * kListEntries * 8 + kDecBytes + 3 * 64 * 4 + 128;
 }
 
 int floats_per_cell(int coil_group)
