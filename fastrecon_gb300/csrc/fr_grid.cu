@@ -137,6 +137,35 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
     const int rows = Ty * Tz;
     const bool pairs = (Tx % 2 == 0) && (P.G % 2 == 0) && ((int)blockDim.x % (Tx / 2) == 0) &&
                        ((reinterpret_cast<uintptr_t>(gridf) & 15) == 0);
+    const int npair = (Tx / 2) * rows;  // x pairs of the tile
+    if (pairs && (int)blockDim.x % npair == 0) {
+        // Each thread keeps one x pair for every coil it writes (coils
+        // tid / npair, + blockDim / npair, ...): the pair's grid offset, its
+        // swizzled columns and checkerboard signs are computed once.
+        const int slot = threadIdx.x % npair, cstep = blockDim.x / npair;
+        const int lx = 2 * (slot % (Tx / 2)), r = slot / (Tx / 2);
+        const int gx = ox + lx, gy = oy + r % Ty, gz = oz + r / Ty;
+        if (gx >= P.G || gy >= P.G || gz >= Gz) return;  // gx even, G even: gx + 1 < G as well
+        float4 *gridc = reinterpret_cast<float4 *>(gridf) + ((((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1);
+        const size_t cstride4 = cells >> 1;  // float4 per coil plane (G even)
+        const int i = r * Tx + lx;
+        const unsigned ra = acc + 4u * (unsigned)(i * R), rb = ra + 4u * (unsigned)R;
+        const int swa = swz<R>(i), swb = swz<R>(i + 1);
+        // (-1)^(x+y+z): opposite signs for x and x+1
+        const float sa = P.checkerboard && ((gx + gy + gz) & 1) ? -1.f : 1.f;
+        const float sb = P.checkerboard ? -sa : 1.f;
+        for (int cl = threadIdx.x / npair; cl < ncl; cl += cstep) {
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!zero) {
+                const int2 a = lds_i32x2(ra + 4u * (unsigned)((2 * cl) ^ swa));
+                const int2 b = lds_i32x2(rb + 4u * (unsigned)((2 * cl) ^ swb));
+                const float ir = inv_scale[2 * cl], ii = inv_scale[2 * cl + 1];
+                v = make_float4((float)a.x * ir * sa, (float)a.y * ii * sa, (float)b.x * ir * sb, (float)b.y * ii * sb);
+            }
+            gridc[(size_t)(cg * CG + cl) * cstride4] = v;
+        }
+        return;
+    }
     if (pairs) {
         const int hx = Tx / 2;
         const int lx = 2 * (threadIdx.x % hx), rr0 = threadIdx.x / hx, rstep = blockDim.x / hx;
