@@ -92,7 +92,9 @@ struct fr_plan_s {
     fr::DevBuf traj;          // n float4, normalised
     fr::DevBuf bounds;        // 16 floats: raw lo/hi as ordered ints, tr, scale, norm lo/hi
     fr::DevBuf tile_count;    // ntiles int
-    fr::DevBuf tile_fill;     // ntiles int
+    fr::DevBuf tile_fill;     // ntiles x stripes int (fill cursors)
+    fr::DevBuf stripe_count;  // ntiles x stripes int (bin counts per stripe)
+    fr::DevBuf stripe_base;   // ntiles x stripes long long (first record of each stripe)
     fr::DevBuf tile_scan;     // (ntiles + 1) TileScan, exclusive
     fr::DevBuf scan_blocks;   // scan scratch
     fr::DevBuf pairs;         // npairs records: sample index | tap box << 32
@@ -159,7 +161,10 @@ struct PlanInto {
     int chunk;
     int *bounds;  // 32 words
     float4 *traj;
-    int *tile_count, *tile_fill;
+    int *tile_count;          // ntiles
+    int *tile_fill;           // ntiles x plan_stripes()
+    int *stripe_count;        // ntiles x plan_stripes()
+    long long *stripe_base;   // ntiles x plan_stripes()
     TileScan *scan;         // ntiles + 1
     TileScan *scan_blocks;  // plan_scan_blocks(ntiles)
     unsigned char *rest;
@@ -173,6 +178,7 @@ struct PlanIntoOut {
     size_t rest_used;
 };
 long long plan_scan_blocks(long long ntiles);
+int plan_stripes();  // bin-counter stripes per tile
 int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s, PlanIntoOut *out);
 
 // Grid from a plan held in caller-provided memory (no allocation).

@@ -99,8 +99,11 @@ extern "C" int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned 
     const size_t off_bounds = align256(off_lut + (size_t)L * 16);
     const size_t off_traj = align256(off_bounds + 32 * 4);
     const size_t off_count = align256(off_traj + std::max<size_t>(n, 1) * 16);
+    const long long nstripes = ntiles * plan_stripes();
     const size_t off_fill = align256(off_count + (size_t)ntiles * 4);
-    const size_t off_scan = align256(off_fill + (size_t)ntiles * 4);
+    const size_t off_scount = align256(off_fill + (size_t)nstripes * 4);
+    const size_t off_sbase = align256(off_scount + (size_t)nstripes * 4);
+    const size_t off_scan = align256(off_sbase + (size_t)nstripes * 8);
     const size_t off_sblk = align256(off_scan + (size_t)(ntiles + 1) * sizeof(TileScan));
     const size_t off_rest = align256(off_sblk + (size_t)nblocks * sizeof(TileScan));
     if (off_rest > FR_NOALLOC_SCRATCH_BYTES)
@@ -140,6 +143,8 @@ extern "C" int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned 
     pi.traj = reinterpret_cast<float4 *>(scratch + off_traj);
     pi.tile_count = reinterpret_cast<int *>(scratch + off_count);
     pi.tile_fill = reinterpret_cast<int *>(scratch + off_fill);
+    pi.stripe_count = reinterpret_cast<int *>(scratch + off_scount);
+    pi.stripe_base = reinterpret_cast<long long *>(scratch + off_sbase);
     pi.scan = reinterpret_cast<TileScan *>(scratch + off_scan);
     pi.scan_blocks = reinterpret_cast<TileScan *>(scratch + off_sblk);
     pi.rest = scratch + off_rest;

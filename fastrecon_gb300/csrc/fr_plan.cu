@@ -160,6 +160,43 @@ __device__ __forceinline__ int tile_of(const BinGeom &g, const int *lo, const in
     return (tz * g.ntile[1] + ty) * g.ntile[0] + tx;
 }
 
+// Bin counters are striped: the samples of 32-sample group g count into
+// stripe g mod kStripes of a tile, so the many warps whose spokes all cross
+// the dense centre tiles spread their atomics over kStripes counters.  A
+// tile's records stay contiguous (stripe-major within the tile).
+constexpr int kStripes = 8;
+__device__ __forceinline__ int stripe_of(size_t first_sample_of_warp)
+{
+    return (int)((first_sample_of_warp >> 5) & (kStripes - 1));
+}
+
+// Tile totals from the stripe counters.
+__global__ void stripe_total_kernel(const int *__restrict__ stripe_count, long long ntiles, int *__restrict__ tile_count)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntiles;
+         t += (long long)gridDim.x * blockDim.x) {
+        int c = 0;
+#pragma unroll
+        for (int k = 0; k < kStripes; ++k) c += stripe_count[t * kStripes + k];
+        tile_count[t] = c;
+    }
+}
+
+// First record of every (tile, stripe) from the scanned tile offsets.
+__global__ void stripe_base_kernel(const int *__restrict__ stripe_count, const TileScan *__restrict__ scan,
+                                   long long ntiles, long long *__restrict__ stripe_base)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntiles;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long o = scan[t].pairs;
+#pragma unroll
+        for (int k = 0; k < kStripes; ++k) {
+            stripe_base[t * kStripes + k] = o;
+            o += stripe_count[t * kStripes + k];
+        }
+    }
+}
+
 // Pass 1: normalise, store the normalised trajectory, count samples per
 // tile.  Counts are aggregated per warp over lanes that hit the same tile
 // (consecutive samples of a readout usually do), so a dense tile sees one
@@ -189,9 +226,8 @@ __global__ void normalize_kernel(const float4 *__restrict__ raw, size_t n, int d
         out[i] = normalize_point(raw[i], dim, tr, scale, 0);
 }
 
-__global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n, BinGeom g,
-                                       const int *__restrict__ b, int prenorm, float4 *__restrict__ out,
-                                       int *__restrict__ tile_count)
+__global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n, BinGeom g, int *b, int prenorm,
+                                       float4 *__restrict__ out, int *__restrict__ stripe_count)
 {
     const float *bf = reinterpret_cast<const float *>(b);
     const float tr = bf[kTr], scale = bf[kScale];
@@ -212,7 +248,7 @@ __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n,
             int t = valid ? tile_of(g, lo, hi, j) : -1 - lane;
             unsigned m = __match_any_sync(0xffffffffu, t);
             int leader = __ffs(m) - 1;
-            if (valid && lane == leader) atomicAdd(&tile_count[t], __popc(m));
+            if (valid && lane == leader) atomicAdd(&stripe_count[t * kStripes + stripe_of(base + threadIdx.x - lane)], __popc(m));
         }
     }
 }
@@ -247,7 +283,7 @@ __device__ __forceinline__ unsigned tile_box(const BinGeom &g, const float *c, c
 
 // Pass 3: fill the sorted bin lists with (sample index, tap box) records.
 __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g,
-                            const TileScan *__restrict__ scan, int *__restrict__ tile_fill,
+                            const long long *__restrict__ stripe_base, int *__restrict__ tile_fill,
                             unsigned long long *__restrict__ recs)
 {
     const int lane = threadIdx.x & 31;
@@ -274,10 +310,11 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
             unsigned m = __match_any_sync(0xffffffffu, t);
             int leader = __ffs(m) - 1;
             int basepos = 0;
-            if (valid && lane == leader) basepos = atomicAdd(&tile_fill[t], __popc(m));
+            const int ts = t * kStripes + stripe_of(base + threadIdx.x - lane);
+            if (valid && lane == leader) basepos = atomicAdd(&tile_fill[ts], __popc(m));
             basepos = __shfl_sync(0xffffffffu, basepos, leader);
             if (valid) {
-                long long pos = scan[t].pairs + basepos + __popc(m & lt);
+                long long pos = stripe_base[ts] + basepos + __popc(m & lt);
                 int tx = t % g.ntile[0];
                 int ty = (t / g.ntile[0]) % g.ntile[1];
                 int tz = t / (g.ntile[0] * g.ntile[1]);
@@ -464,15 +501,16 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     p->n = n;
     if (p->bounds.reserve(kBoundsSlots * 4)) return FR_ERR_OUT_OF_MEMORY;
     if (p->traj.reserve(std::max<size_t>(n, 1) * 16)) return FR_ERR_OUT_OF_MEMORY;
-    if (p->tile_count.reserve(p->ntiles * 4) || p->tile_fill.reserve(p->ntiles * 4) ||
+    if (p->tile_count.reserve(p->ntiles * 4) || p->tile_fill.reserve(p->ntiles * kStripes * 4) ||
+        p->stripe_count.reserve(p->ntiles * kStripes * 4) || p->stripe_base.reserve(p->ntiles * kStripes * 8) ||
         p->tile_scan.reserve((p->ntiles + 1) * sizeof(TileScan)))
         return FR_ERR_OUT_OF_MEMORY;
     long long nblocks = (p->ntiles + kScanSeg - 1) / kScanSeg;
     if (p->scan_blocks.reserve(std::max<long long>(nblocks, 1) * sizeof(TileScan))) return FR_ERR_OUT_OF_MEMORY;
 
     int *b = p->bounds.as<int>();
-    FR_CUDA(cudaMemsetAsync(p->tile_count.ptr, 0, p->ntiles * 4, s));
-    FR_CUDA(cudaMemsetAsync(p->tile_fill.ptr, 0, p->ntiles * 4, s));
+    FR_CUDA(cudaMemsetAsync(p->stripe_count.ptr, 0, p->ntiles * kStripes * 4, s));
+    FR_CUDA(cudaMemsetAsync(p->tile_fill.ptr, 0, p->ntiles * kStripes * 4, s));
     bounds_init_kernel<<<1, 32, 0, s>>>(b);
     FR_CHECK_LAUNCH("bounds_init_kernel");
     const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
@@ -495,9 +533,12 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     float4 *traj = p->traj.as<float4>();
     if (n > 0) {
         normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(
-            raw, n, g, b, (p->flags & FR_PLAN_PRENORMALIZED) ? 1 : 0, traj, p->tile_count.as<int>());
+            raw, n, g, b, (p->flags & FR_PLAN_PRENORMALIZED) ? 1 : 0, traj, p->stripe_count.as<int>());
         FR_CHECK_LAUNCH("normalize_count_kernel");
     }
+    stripe_total_kernel<<<grid_blocks(p->ntiles, 256), 256, 0, s>>>(p->stripe_count.as<int>(), p->ntiles,
+                                                                    p->tile_count.as<int>());
+    FR_CHECK_LAUNCH("stripe_total_kernel");
     TileScan *bs = p->scan_blocks.as<TileScan>();
     TileScan *scan = p->tile_scan.as<TileScan>();
     scan_reduce_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(p->tile_count.as<int>(), p->ntiles, p->chunk, bs);
@@ -507,6 +548,9 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     scan_write_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(p->tile_count.as<int>(), p->ntiles, p->chunk, bs,
                                                             scan);
     FR_CHECK_LAUNCH("scan_write_kernel");
+    stripe_base_kernel<<<grid_blocks(p->ntiles, 256), 256, 0, s>>>(p->stripe_count.as<int>(), scan, p->ntiles,
+                                                                   p->stripe_base.as<long long>());
+    FR_CHECK_LAUNCH("stripe_base_kernel");
 
     TileScan tot;
     FR_CUDA(cudaMemcpyAsync(&tot, scan + p->ntiles, sizeof(TileScan), cudaMemcpyDeviceToHost, s));
@@ -533,7 +577,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         p->splits.reserve(std::max<long long>(tot.splits, 1) * sizeof(SplitTile)))
         return FR_ERR_OUT_OF_MEMORY;
     if (n > 0) {
-        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, scan, p->tile_fill.as<int>(),
+        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, p->stripe_base.as<long long>(), p->tile_fill.as<int>(),
                                                         p->pairs.as<unsigned long long>());
         FR_CHECK_LAUNCH("fill_kernel");
     }
@@ -598,6 +642,8 @@ int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_o
     return FR_OK;
 }
 
+int plan_stripes() { return kStripes; }
+
 long long plan_scan_blocks(long long ntiles)
 {
     return std::max<long long>((ntiles + kScanSeg - 1) / kScanSeg, 1);
@@ -608,8 +654,8 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
 {
     const long long nblocks = (pi.ntiles + kScanSeg - 1) / kScanSeg;
     int *b = pi.bounds;
-    FR_CUDA(cudaMemsetAsync(pi.tile_count, 0, pi.ntiles * 4, s));
-    FR_CUDA(cudaMemsetAsync(pi.tile_fill, 0, pi.ntiles * 4, s));
+    FR_CUDA(cudaMemsetAsync(pi.stripe_count, 0, pi.ntiles * kStripes * 4, s));
+    FR_CUDA(cudaMemsetAsync(pi.tile_fill, 0, pi.ntiles * kStripes * 4, s));
     bounds_init_kernel<<<1, 32, 0, s>>>(b);
     FR_CHECK_LAUNCH("bounds_init_kernel");
     const float4 *raw = reinterpret_cast<const float4 *>(d_traj);
@@ -629,9 +675,11 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
         g.ntile[d] = pi.ntile[d];
     }
     if (n > 0) {
-        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, 0, pi.traj, pi.tile_count);
+        normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, 0, pi.traj, pi.stripe_count);
         FR_CHECK_LAUNCH("normalize_count_kernel");
     }
+    stripe_total_kernel<<<grid_blocks(pi.ntiles, 256), 256, 0, s>>>(pi.stripe_count, pi.ntiles, pi.tile_count);
+    FR_CHECK_LAUNCH("stripe_total_kernel");
     scan_reduce_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(pi.tile_count, pi.ntiles, pi.chunk, pi.scan_blocks);
     FR_CHECK_LAUNCH("scan_reduce_kernel");
     scan_blocks_kernel<<<1, kScanThreads, 0, s>>>(pi.scan_blocks, (int)nblocks);
@@ -639,6 +687,9 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
     scan_write_kernel<<<(int)nblocks, kScanThreads, 0, s>>>(pi.tile_count, pi.ntiles, pi.chunk, pi.scan_blocks,
                                                             pi.scan);
     FR_CHECK_LAUNCH("scan_write_kernel");
+    stripe_base_kernel<<<grid_blocks(pi.ntiles, 256), 256, 0, s>>>(pi.stripe_count, pi.scan, pi.ntiles,
+                                                                   pi.stripe_base);
+    FR_CHECK_LAUNCH("stripe_base_kernel");
     TileScan tot;
     FR_CUDA(cudaMemcpyAsync(&tot, pi.scan + pi.ntiles, sizeof(TileScan), cudaMemcpyDeviceToHost, s));
     FR_CUDA(cudaStreamSynchronize(s));
@@ -660,7 +711,7 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
     out->splits = reinterpret_cast<SplitTile *>(pi.rest + recs_b + items_b);
     out->rest_used = recs_b + items_b + splits_b;
     if (n > 0) {
-        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(pi.traj, n, g, pi.scan, pi.tile_fill, out->recs);
+        fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(pi.traj, n, g, pi.stripe_base, pi.tile_fill, out->recs);
         FR_CHECK_LAUNCH("fill_kernel");
     }
     items_kernel<<<grid_blocks(pi.ntiles, 256), 256, 0, s>>>(pi.tile_count, pi.scan, pi.ntiles, pi.chunk, out->items,
