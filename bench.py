@@ -44,6 +44,10 @@ WORKLOADS = {
                              dcf_power=2.0,
                              desc="reduced 3D kooshball for profiling: 12,500 golden-means spokes x 128 samples, "
                                   "16 coils, os 1.5 -> 192^3 grid"),
+    # the kooshball's 384^3 transform with 2 coils (0.9 GB grid), for ncu captures of the FFT stages
+    "kooshball3d_fft": dict(dim=3, spokes=2000, readout=256, coils=2, recon=256, os=1.5, width=4.0, lut=512,
+                            dcf_power=2.0,
+                            desc="3D kooshball, 2,000 spokes x 256, 2 coils, os 1.5 -> 384^3 grid (FFT profiling)"),
     "radial2d": dict(dim=2, spokes=256, readout=512, coils=8, recon=256, os=2.0, width=4.0, lut=512,
                      dcf_power=1.0,
                      desc="2D radial: 256 spokes x 512 samples, 8 coils, |k| DCF, KB width 4, LUT 512, "

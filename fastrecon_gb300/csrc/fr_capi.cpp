@@ -274,6 +274,10 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
     }
     p->chunk = d->chunk > 0 ? d->chunk : 4096;
     {
+        const char *cm = std::getenv("FR_KSPACE_COIL_MAJOR");
+        p->kspace_sample_major = !(cm && std::atoi(cm) != 0);
+    }
+    {
         // exact when hw^2 is representable and sqrt rounds back to hw
         float h2 = p->hw * p->hw;
         p->prefilter = (std::sqrt(h2) == p->hw) && ((double)h2 == (double)p->hw * (double)p->hw);

@@ -52,6 +52,10 @@ struct GridParams {
     int *work_counter;  // persistent kernel: next work index
     long long nwork;    // persistent kernel: nitems * ngroups
     float lut_absmax;   // max |lut[k]|: bounds every tap weight
+    // k-space sample-major ([n][channels] complex, from transpose_kspace):
+    // a record's coil values are one contiguous run instead of one value per
+    // coil plane
+    int sample_major;
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -105,6 +109,12 @@ __device__ __forceinline__ int2 lds_s32x2(unsigned a)
 {
     int2 r;
     asm volatile("ld.shared.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "r"(a) : "memory");
+    return r;
+}
+__device__ __forceinline__ unsigned lds_u32(unsigned a)
+{
+    unsigned r;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
     return r;
 }
 __device__ __forceinline__ float4 lds_f32x4(unsigned a)
@@ -234,24 +244,25 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
 constexpr int kScaleBatch = 4;     // records per warp step of the scale pass
-constexpr int kDecBytes = 16 * 64 * 16;  // tap decode table: 16 box classes x 64 taps x float4
+constexpr int kDecBytes = 16 * 64 * 4;  // tap decode table: 16 box classes x 64 taps x 32-bit word
 
 // Shared-memory layout of the scatter: accumulator tile [K][R] int32 | LUT
 // entries [L] float4 | per warp two tap-list buffers [32] {shared address of
-// the tap's cell row (swizzled), weight} | tap decode table [16][64] float4 |
+// the tap's cell row (swizzled), weight} | tap decode table [16][64] words |
 // per coil float: bound sum, bound max, inverse scale [3][64] floats.
 //
 // Decode table: for a tap box of nx x ny x nz cells (nx, ny <= 4; class
-// (nx-1)*4 + (ny-1)), tap tt = ix + nx (iy + ny iz) is {ix, iy, iz, cell
-// offset (iz Ty + iy) Tx + ix} with the offsets as floats (exact) and the cell
-// offset as integer bits.  Built without divisions: t / n for n <= 4 and
-// t < 64 is (t * {128, 64, 43, 32}[n-1]) >> 7.
+// (nx-1)*4 + (ny-1)), tap tt = ix + nx (iy + ny iz) is the word ix | iy << 4 |
+// iz << 8 | cell offset ((iz Ty + iy) Tx + ix) << 12: one 4-byte entry per
+// lane keeps the lookup at one shared-memory wavefront per warp.  Built
+// without divisions: t / n for n <= 4 and t < 64 is
+// (t * {128, 64, 43, 32}[n-1]) >> 7.
 template <int R>
 __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
 {
     float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)P.K * R);
-    float4 *dec_g = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(lutE_g + P.L) +
-                                               kWarps * 2 * kListEntries * 8);
+    unsigned *dec_g = reinterpret_cast<unsigned *>(reinterpret_cast<unsigned char *>(lutE_g + P.L) +
+                                                   kWarps * 2 * kListEntries * 8);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutE_g[i] = P.lut_e[i];
     const int Tx = P.tile[0], Ty = P.tile[1];
     for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
@@ -261,7 +272,91 @@ __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
         const int my = ny == 1 ? 128 : ny == 2 ? 64 : ny == 3 ? 43 : 32;
         const int q1 = (tt * mx) >> 7, ix = tt - q1 * nx;
         const int iz = (q1 * my) >> 7, iy = q1 - iz * ny;
-        dec_g[i] = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
+        dec_g[i] = (unsigned)ix | ((unsigned)iy << 4) | ((unsigned)iz << 8) | ((unsigned)((iz * Ty + iy) * Tx + ix) << 12);
+    }
+}
+
+// Scale of the fixed-point tile, per coil float f: with B_f = sum and
+// M_f = max over the item's samples of |dcf * k_f|, and |w| <= lut_absmax,
+// every partial sum is below B_f * lut_absmax and every add below
+// M_f * lut_absmax, so S_f = the largest power of two with
+// S_f * B_f * lut_absmax <= 2^30 and S_f * M_f * lut_absmax <= 2^21 keeps
+// the tile in int32 and each add exact to +-1/2.  The rounding error of an
+// add is then at most B_f / 2^31 (dense items) or 2^-23 M_f.
+//
+// This warp's part of B_f and M_f over records warp, warp + NW, ... in steps
+// of kScaleBatch records with every load of a step issued before the first
+// is used (the pass is bound by the latency of these gathers).  PF: lane b of
+// a step also pulls record b's position into L1 for the accumulation pass.
+template <int NF, int NW, bool PF>
+__device__ __forceinline__ void scale_bounds(const unsigned long long *recs, int count, int warp, int lane,
+                                             const float4 *traj, const float *dcf, const float *const *kdf,
+                                             size_t ks, const bool *coil_ok, float *bs, float *bm)
+{
+#pragma unroll
+    for (int k = 0; k < NF; ++k) bs[k] = bm[k] = 0.f;
+    for (int j0 = warp * kScaleBatch; j0 < count; j0 += NW * kScaleBatch) {
+        unsigned sl = 0u;
+        bool vl = false;
+        if (lane < kScaleBatch && j0 + lane < count) {
+            const unsigned long long rec = recs[j0 + lane];
+            const unsigned box = (unsigned)(rec >> 32);
+            sl = (unsigned)rec;
+            vl = ((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) != 0;
+            if (PF && vl) asm volatile("prefetch.global.L1 [%0];" ::"l"(traj + sl));
+        }
+        const unsigned vm = __ballot_sync(0xffffffffu, vl);
+        float db[kScaleBatch], kb[kScaleBatch][NF];
+#pragma unroll
+        for (int b = 0; b < kScaleBatch; ++b) {
+            const unsigned sv = __shfl_sync(0xffffffffu, sl, b);
+            const bool v = (vm >> b) & 1u;
+            db[b] = v ? dcf[sv] : 0.f;
+#pragma unroll
+            for (int k = 0; k < NF; ++k) kb[b][k] = v && coil_ok[k] ? kdf[k][ks * sv] : 0.f;
+        }
+#pragma unroll
+        for (int b = 0; b < kScaleBatch; ++b) {
+#pragma unroll
+            for (int k = 0; k < NF; ++k) {
+                const float a = fabsf(__fmul_rn(db[b], kb[b][k]));
+                bs[k] += a;
+                bm[k] = fmaxf(bm[k], a);
+            }
+        }
+    }
+}
+
+// 1 / S_f from the item's B_f and M_f (exact: a power of two).
+__device__ __forceinline__ float inv_scale_of(float bsum, unsigned bmax_bits, float lut_absmax)
+{
+    const float B = __fmul_rn(bsum, lut_absmax);
+    const float M = __fmul_rn(__uint_as_float(bmax_bits), lut_absmax);
+    int e = 0;
+    if (B > 0.f && M > 0.f) {
+        // largest power of two 2^e <= min(2^30 / B, 2^21 / M)
+        const float t = fminf(__fdiv_rn(1073741824.f, B), __fdiv_rn(2097152.f, M));
+        frexpf(t, &e);
+        e = max(min(e - 1, 100), -100);
+    }
+    return ldexpf(1.f, -e);
+}
+
+// The k-space pointers of a lane: kdf[k][ks s] is coil float f0 + 32 k of
+// sample s (coil_ok false past the group's or the data's last coil), ks = 2
+// for coil-major k-space, 2 * channels for sample-major.
+template <int NF>
+__device__ __forceinline__ void lane_kspace(const GridParams &P, int cg, int f0, long long s_off, long long n_f,
+                                            const float **kdf, bool *coil_ok)
+{
+    const int CG = P.coil_group;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+        const int fl = f0 + 32 * k;
+        const int coil = cg * CG + (fl >> 1);
+        coil_ok[k] = (fl >> 1) < CG && coil < P.channels;
+        kdf[k] = P.kdata + 2 * (size_t)P.channels * (size_t)s_off +
+                 2 * (size_t)(coil_ok[k] ? coil : 0) * (P.sample_major ? (size_t)1 : (size_t)n_f) + (fl & 1);
     }
 }
 
@@ -313,69 +408,19 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     const int q = R >= 32 ? 0 : lane / R;     // tap slot of this lane
     const int f0 = R >= 32 ? lane : lane % R; // first coil float of this lane
     const unsigned f0b = (unsigned)f0 << 2;   // its byte offset in a cell row
-    const int CG = P.coil_group;
     const int Tx = P.tile[0], Ty = P.tile[1];
     const unsigned mylist = lists + (unsigned)(warp * 2 * kListEntries * 8);
     unsigned buf = 0;
 
     const float *kdf[NF];
     bool coil_ok[NF];
-#pragma unroll
-    for (int k = 0; k < NF; ++k) {
-        const int fl = f0 + 32 * k;
-        const int coil = cg * CG + (fl >> 1);
-        coil_ok[k] = (fl >> 1) < CG && coil < P.channels;
-        // real or imaginary float of this coil's sample s is kdf[k][2 * s]
-        kdf[k] = P.kdata + 2 * (size_t)P.channels * (size_t)s_off +
-                 2 * (size_t)(coil_ok[k] ? coil : 0) * (size_t)n_f + (fl & 1);
-    }
+    lane_kspace<NF>(P, cg, f0, s_off, n_f, kdf, coil_ok);
+    const size_t ks = P.sample_major ? 2 * (size_t)P.channels : 2;
     const unsigned long long *recs = P.recs + it.begin;
 
-    // Scale of the fixed-point tile, per coil float f: with B_f = sum and
-    // M_f = max over the item's samples of |dcf * k_f|, and |w| <= lut_absmax,
-    // every partial sum is below B_f * lut_absmax and every add below
-    // M_f * lut_absmax, so S_f = the largest power of two with
-    // S_f * B_f * lut_absmax <= 2^30 and S_f * M_f * lut_absmax <= 2^21 keeps
-    // the tile in int32 and each add exact to +-1/2.  The rounding error of
-    // an add is then at most B_f / 2^31 (dense items) or 2^-23 M_f.
     {
         float bs[NF], bm[NF];
-#pragma unroll
-        for (int k = 0; k < NF; ++k) bs[k] = bm[k] = 0.f;
-        // kScaleBatch records per warp step, every load of the step issued
-        // before the first is used (the pass is bound by the latency of these
-        // gathers); lane b of the step also pulls record b's position into L1
-        // for the accumulation pass.
-        for (int j0 = warp * kScaleBatch; j0 < it.count; j0 += kWarps * kScaleBatch) {
-            unsigned sl = 0u;
-            bool vl = false;
-            if (lane < kScaleBatch && j0 + lane < it.count) {
-                const unsigned long long rec = recs[j0 + lane];
-                const unsigned box = (unsigned)(rec >> 32);
-                sl = (unsigned)rec;
-                vl = ((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) != 0;
-                if (vl) asm volatile("prefetch.global.L1 [%0];" ::"l"(traj + sl));
-            }
-            const unsigned vm = __ballot_sync(0xffffffffu, vl);
-            float db[kScaleBatch], kb[kScaleBatch][NF];
-#pragma unroll
-            for (int b = 0; b < kScaleBatch; ++b) {
-                const unsigned sv = __shfl_sync(0xffffffffu, sl, b);
-                const bool v = (vm >> b) & 1u;
-                db[b] = v ? dcf[sv] : 0.f;
-#pragma unroll
-                for (int k = 0; k < NF; ++k) kb[b][k] = v && coil_ok[k] ? kdf[k][2 * (size_t)sv] : 0.f;
-            }
-#pragma unroll
-            for (int b = 0; b < kScaleBatch; ++b) {
-#pragma unroll
-                for (int k = 0; k < NF; ++k) {
-                    const float a = fabsf(__fmul_rn(db[b], kb[b][k]));
-                    bs[k] += a;
-                    bm[k] = fmaxf(bm[k], a);
-                }
-            }
-        }
+        scale_bounds<NF, kWarps, true>(recs, it.count, warp, lane, traj, dcf, kdf, ks, coil_ok, bs, bm);
         if (q == 0) {
 #pragma unroll
             for (int k = 0; k < NF; ++k) {
@@ -386,18 +431,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             }
         }
         __syncthreads();
-        if (threadIdx.x < R) {
-            const float B = __fmul_rn(bsum_s[threadIdx.x], P.lut_absmax);
-            const float M = __fmul_rn(__uint_as_float(bmax_s[threadIdx.x]), P.lut_absmax);
-            int e = 0;
-            if (B > 0.f && M > 0.f) {
-                // largest power of two 2^e <= min(2^30 / B, 2^21 / M)
-                const float t = fminf(__fdiv_rn(1073741824.f, B), __fdiv_rn(2097152.f, M));
-                frexpf(t, &e);
-                e = max(min(e - 1, 100), -100);
-            }
-            inv_s[threadIdx.x] = ldexpf(1.f, -e);  // exact: a power of two
-        }
+        if (threadIdx.x < R) inv_s[threadIdx.x] = inv_scale_of(bsum_s[threadIdx.x], bmax_s[threadIdx.x], P.lut_absmax);
         __syncthreads();
     }
     float sc[NF];
@@ -419,9 +453,9 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         float val[NF];
 #pragma unroll
         for (int k = 0; k < NF; ++k)
-            val[k] = coil_ok[k] ? __fmul_rn(__fmul_rn(d, kdf[k][2 * (size_t)s]), sc[k]) : 0.f;  // GridLut.cpp:109, scaled
+            val[k] = coil_ok[k] ? __fmul_rn(__fmul_rn(d, kdf[k][ks * s]), sc[k]) : 0.f;  // GridLut.cpp:109, scaled
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
-        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 16);
+        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 4);
         // box origin as floats (integers below 2^24: exact), its first cell
         const float fgx = (float)(ox + lx0), fgy = (float)(oy + ly0), fgz = (float)(oz + lz0);
         const int cell0 = (lz0 * Ty + ly0) * Tx + lx0;
@@ -432,7 +466,9 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             const int tt = rnd * 32 + lane;
             float4 d4;
             if (small) {  // warp-uniform; nround <= 2, so tt < 64
-                d4 = lds_f32x4(dtab + 16u * (unsigned)tt);
+                const unsigned c = lds_u32(dtab + 4u * (unsigned)tt);
+                d4 = make_float4((float)(c & 15u), (float)((c >> 4) & 15u), (float)((c >> 8) & 15u),
+                                 __int_as_float((int)(c >> 12)));
             } else {
                 const int ix = tt % nx, r = tt / nx, iy = r % ny, iz = r / ny;
                 d4 = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
@@ -595,6 +631,26 @@ __global__ void reduce_splits_kernel(GridParams P)
     }
 }
 
+// [channels][n] complex -> [n][channels] complex, kTrSamples samples per CTA
+// through shared memory (coalesced reads along n, writes along channels).
+constexpr int kTrSamples = 128;
+__global__ void __launch_bounds__(256) transpose_kspace_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                                               long long n, int channels)
+{
+    extern __shared__ float2 tr[];  // [channels][kTrSamples + 1]
+    const long long s0 = (long long)blockIdx.x * kTrSamples;
+    const int ns = (int)min((long long)kTrSamples, n - s0);
+    for (int i = threadIdx.x; i < channels * kTrSamples; i += blockDim.x) {
+        const int c = i / kTrSamples, j = i - c * kTrSamples;
+        if (j < ns) tr[c * (kTrSamples + 1) + j] = in[(size_t)c * n + s0 + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < channels * ns; i += blockDim.x) {
+        const int j = i / channels, c = i - j * channels;
+        out[(size_t)(s0 + j) * channels + c] = tr[c * (kTrSamples + 1) + j];
+    }
+}
+
 template <int DIM, int R>
 int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, cudaStream_t s)
 {
@@ -695,6 +751,19 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.grid_frame_floats = 0;
     P.work_counter = nullptr;
     P.nwork = 0;
+    P.sample_major = 0;
+    const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
+    if (p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024) {
+        if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2))) return FR_ERR_OUT_OF_MEMORY;
+        if (trsmem > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsmem));
+        transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), 256, trsmem, s>>>(
+            reinterpret_cast<const float2 *>(d_kdata), p->kt.as<float2>(), (long long)p->n, channels);
+        FR_CHECK_LAUNCH("transpose_kspace_kernel");
+        P.kdata = p->kt.as<float>();
+        P.sample_major = 1;
+    }
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;
         if (p->partials.reserve(bytes)) return FR_ERR_OUT_OF_MEMORY;
@@ -784,6 +853,7 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.grid_frame_floats = 0;
     P.work_counter = nullptr;
     P.nwork = 0;
+    P.sample_major = 0;
     if (gi.nitems == 0) return FR_OK;
     if (gi.dim == 3) {
         switch (R) {
@@ -896,6 +966,7 @@ int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf,
     P.grid_frame_floats = (long long)(2 * (size_t)channels * cells);
     P.work_counter = b.work_counter;
     P.nwork = b.nitems * P.ngroups;
+    P.sample_major = 0;
     if (P.nwork == 0) return FR_OK;
     if (P.nwork > 0x7FFFFFFFll) return fail(FR_ERR_UNSUPPORTED, "too many work items");
     if (b.dim == 3) {
