@@ -126,38 +126,55 @@ struct BinGeom {
     int prefilter;
     int tile[3];
     int ntile[3];
+    int tshift[3];  // log2(tile[d]) for power-of-two tiles, else -1
 };
 
-// Normalise one sample (ReconData.cpp:201-209: (x + tr) * scale) and find
-// the tiles its clamped cell range touches.  Returns the number of tiles;
-// lo/hi receive the tile-coordinate box.
-__device__ __forceinline__ int sample_tiles(const BinGeom &g, float4 &p, int *lo, int *hi)
+// Cell index -> tile index along axis d (x >= 0).
+__device__ __forceinline__ int tile_div(const BinGeom &g, int x, int d)
 {
-    float c[3] = {p.x, p.y, p.z};
+    return g.tshift[d] >= 0 ? x >> g.tshift[d] : x / g.tile[d];
+}
+
+// The tiles of one sample's cell range, visited in x, y, z order by an
+// odometer (no divisions per step).
+struct TileWalk {
+    int lo[3], n[3];
+    int jx = 0, jy = 0, jz = 0;
+    __device__ __forceinline__ void next()
+    {
+        if (++jx == n[0]) {
+            jx = 0;
+            if (++jy == n[1]) {
+                jy = 0;
+                ++jz;
+            }
+        }
+    }
+    __device__ __forceinline__ int tile(const BinGeom &g) const
+    {
+        return ((lo[2] + jz) * g.ntile[1] + lo[1] + jy) * g.ntile[0] + lo[0] + jx;
+    }
+};
+
+// Find the tiles a sample's clamped cell range touches (s/e: the range,
+// GridLut.cpp:98-106).  Returns the number of tiles and sets up the walk.
+__device__ __forceinline__ int sample_tiles(const BinGeom &g, const float4 &p, TileWalk &w, int *s, int *e)
+{
+    const float c[3] = {p.x, p.y, p.z};
     int cnt = 1;
     for (int d = 0; d < 3; ++d) {
         if (d < g.dim) {
-            int s, e;
-            comp_range(c[d], g.hw, g.G, s, e);
-            if (s > e) cnt = 0;
-            lo[d] = s / g.tile[d];
-            hi[d] = e / g.tile[d];
+            comp_range(c[d], g.hw, g.G, s[d], e[d]);
+            if (s[d] > e[d]) cnt = 0;
         } else {
-            lo[d] = hi[d] = 0;
+            s[d] = e[d] = 0;
         }
     }
-    if (cnt) cnt = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-    return cnt;
-}
-
-__device__ __forceinline__ int tile_of(const BinGeom &g, const int *lo, const int *hi, int j)
-{
-    int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
-    int tx = lo[0] + j % nx;
-    int r = j / nx;
-    int ty = lo[1] + r % ny;
-    int tz = lo[2] + r / ny;
-    return (tz * g.ntile[1] + ty) * g.ntile[0] + tx;
+    for (int d = 0; d < 3; ++d) {
+        w.lo[d] = cnt ? tile_div(g, s[d], d) : 0;
+        w.n[d] = cnt ? tile_div(g, e[d], d) - w.lo[d] + 1 : 1;
+    }
+    return cnt ? w.n[0] * w.n[1] * w.n[2] : 0;
 }
 
 // Bin counters are striped: the samples of 32-sample group g count into
@@ -235,20 +252,25 @@ __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n,
     for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n;
          base += (size_t)gridDim.x * blockDim.x) {
         size_t i = base + threadIdx.x;
-        int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
+        TileWalk w;
+        int s[3], e[3];
         int cnt = 0;
         if (i < n) {
             float4 q = normalize_point(raw[i], g.dim, tr, scale, prenorm);
             out[i] = q;
-            cnt = sample_tiles(g, q, lo, hi);
+            cnt = sample_tiles(g, q, w, s, e);
+        } else {
+            w.lo[0] = w.lo[1] = w.lo[2] = 0;
+            w.n[0] = w.n[1] = w.n[2] = 1;
         }
+        const int stripe = stripe_of(base + threadIdx.x - lane);
         int maxcnt = __reduce_max_sync(0xffffffffu, cnt);
-        for (int j = 0; j < maxcnt; ++j) {
+        for (int j = 0; j < maxcnt; ++j, w.next()) {
             bool valid = j < cnt;
-            int t = valid ? tile_of(g, lo, hi, j) : -1 - lane;
+            int t = valid ? w.tile(g) : -1 - lane;
             unsigned m = __match_any_sync(0xffffffffu, t);
             int leader = __ffs(m) - 1;
-            if (valid && lane == leader) atomicAdd(&stripe_count[t * kStripes + stripe_of(base + threadIdx.x - lane)], __popc(m));
+            if (valid && lane == leader) atomicAdd(&stripe_count[t * kStripes + stripe], __popc(m));
         }
     }
 }
@@ -291,34 +313,34 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
     for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n;
          base += (size_t)gridDim.x * blockDim.x) {
         size_t i = base + threadIdx.x;
-        int lo[3] = {0, 0, 0}, hi[3] = {-1, 0, 0};
+        TileWalk w;
         int s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
         float c[3] = {0.f, 0.f, 0.f};
         int cnt = 0;
         if (i < n) {
             float4 q = traj[i];
-            cnt = sample_tiles(g, q, lo, hi);
+            cnt = sample_tiles(g, q, w, s, e);
             c[0] = q.x;
             c[1] = q.y;
             c[2] = q.z;
-            for (int d = 0; d < g.dim; ++d) comp_range(c[d], g.hw, g.G, s[d], e[d]);
+        } else {
+            w.lo[0] = w.lo[1] = w.lo[2] = 0;
+            w.n[0] = w.n[1] = w.n[2] = 1;
         }
+        const int stripe = stripe_of(base + threadIdx.x - lane);
         int maxcnt = __reduce_max_sync(0xffffffffu, cnt);
-        for (int j = 0; j < maxcnt; ++j) {
+        for (int j = 0; j < maxcnt; ++j, w.next()) {
             bool valid = j < cnt;
-            int t = valid ? tile_of(g, lo, hi, j) : -1 - lane;
+            int t = valid ? w.tile(g) : -1 - lane;
             unsigned m = __match_any_sync(0xffffffffu, t);
             int leader = __ffs(m) - 1;
             int basepos = 0;
-            const int ts = t * kStripes + stripe_of(base + threadIdx.x - lane);
+            const int ts = t * kStripes + stripe;
             if (valid && lane == leader) basepos = atomicAdd(&tile_fill[ts], __popc(m));
             basepos = __shfl_sync(0xffffffffu, basepos, leader);
             if (valid) {
                 long long pos = stripe_base[ts] + basepos + __popc(m & lt);
-                int tx = t % g.ntile[0];
-                int ty = (t / g.ntile[0]) % g.ntile[1];
-                int tz = t / (g.ntile[0] * g.ntile[1]);
-                unsigned box = tile_box(g, c, s, e, tx, ty, tz);
+                unsigned box = tile_box(g, c, s, e, w.lo[0] + w.jx, w.lo[1] + w.jy, w.lo[2] + w.jz);
                 recs[pos] = ((unsigned long long)box << 32) | (unsigned long long)i;
             }
         }
@@ -529,6 +551,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     for (int d = 0; d < 3; ++d) {
         g.tile[d] = p->tile[d];
         g.ntile[d] = p->ntile[d];
+        g.tshift[d] = (g.tile[d] & (g.tile[d] - 1)) == 0 ? __builtin_ctz((unsigned)g.tile[d]) : -1;
     }
     float4 *traj = p->traj.as<float4>();
     if (n > 0) {
@@ -673,6 +696,7 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
     for (int d = 0; d < 3; ++d) {
         g.tile[d] = pi.tile[d];
         g.ntile[d] = pi.ntile[d];
+        g.tshift[d] = (g.tile[d] & (g.tile[d] - 1)) == 0 ? __builtin_ctz((unsigned)g.tile[d]) : -1;
     }
     if (n > 0) {
         normalize_count_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(raw, n, g, b, 0, pi.traj, pi.stripe_count);
