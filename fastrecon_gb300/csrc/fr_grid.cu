@@ -633,19 +633,34 @@ __global__ void reduce_splits_kernel(GridParams P)
 
 // [channels][n] complex -> [n][channels] complex, kTrSamples samples per CTA
 // through shared memory (coalesced reads along n, writes along channels).
+// Each thread issues kTrPer loads before it stores any of them (the copy is
+// bound by the latency of these reads).
 constexpr int kTrSamples = 128;
-__global__ void __launch_bounds__(256) transpose_kspace_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
-                                                               long long n, int channels)
+constexpr int kTrThreads = 256, kTrPer = 8;
+__global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const float2 *__restrict__ in,
+                                                                      float2 *__restrict__ out, long long n,
+                                                                      int channels)
 {
     extern __shared__ float2 tr[];  // [channels][kTrSamples + 1]
     const long long s0 = (long long)blockIdx.x * kTrSamples;
     const int ns = (int)min((long long)kTrSamples, n - s0);
-    for (int i = threadIdx.x; i < channels * kTrSamples; i += blockDim.x) {
-        const int c = i / kTrSamples, j = i - c * kTrSamples;
-        if (j < ns) tr[c * (kTrSamples + 1) + j] = in[(size_t)c * n + s0 + j];
+    const int total = channels * kTrSamples;
+    for (int i0 = 0; i0 < total; i0 += kTrThreads * kTrPer) {
+        float2 v[kTrPer];
+#pragma unroll
+        for (int k = 0; k < kTrPer; ++k) {
+            const int i = i0 + k * kTrThreads + threadIdx.x;
+            const int c = i / kTrSamples, j = i % kTrSamples;
+            v[k] = i < total && j < ns ? in[(size_t)c * n + s0 + j] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < kTrPer; ++k) {
+            const int i = i0 + k * kTrThreads + threadIdx.x;
+            if (i < total) tr[(i / kTrSamples) * (kTrSamples + 1) + i % kTrSamples] = v[k];
+        }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < channels * ns; i += blockDim.x) {
+    for (int i = threadIdx.x; i < channels * ns; i += kTrThreads) {
         const int j = i / channels, c = i - j * channels;
         out[(size_t)(s0 + j) * channels + c] = tr[c * (kTrSamples + 1) + j];
     }
@@ -758,7 +773,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
         if (trsmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsmem));
-        transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), 256, trsmem, s>>>(
+        transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
             reinterpret_cast<const float2 *>(d_kdata), p->kt.as<float2>(), (long long)p->n, channels);
         FR_CHECK_LAUNCH("transpose_kspace_kernel");
         P.kdata = p->kt.as<float>();
