@@ -76,6 +76,7 @@ _SIGS = {
                                     C.c_int, C.POINTER(PlanDesc), C.POINTER(C.c_float), _VP]),
     "fr_dcf_analytic": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_float, _VP, _VP]),
     "fr_degrid": (C.c_int, [_VP, _VP, C.c_int, _VP, _VP]),
+    "fr_grid_update": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.c_size_t, _VP, C.c_int, _VP, _VP]),
     "fr_grid_real": (C.c_int, [_VP, _VP, _VP, _VP]),
     "fr_dcf_pipe": (C.c_int, [_VP, C.c_int, _VP, _VP]),
     "fr_density_counts": (C.c_int, [_VP, C.POINTER(C.c_int), C.c_int, _VP, _VP]),

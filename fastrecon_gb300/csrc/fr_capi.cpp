@@ -432,6 +432,16 @@ int fr_degrid(fr_plan p, const float *d_grid, int channels, float *d_kdata, void
     return degrid_run(p, d_grid, channels, d_kdata, (cudaStream_t)stream);
 }
 
+int fr_grid_update(fr_plan p, float *d_kdata, const float *d_new, size_t sample_begin, size_t count,
+                   const float *d_dcf, int channels, float *d_grid, void *stream)
+{
+    if (!p || (count && (!d_kdata || !d_new || !d_dcf || !d_grid))) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_kdata) & 7) || (reinterpret_cast<uintptr_t>(d_new) & 7) ||
+        (reinterpret_cast<uintptr_t>(d_grid) & 7))
+        return fail(FR_ERR_INVALID_ARGUMENT, "complex buffers must be 8-byte aligned");
+    return grid_update_run(p, d_kdata, d_new, sample_begin, count, d_dcf, channels, d_grid, (cudaStream_t)stream);
+}
+
 int fr_grid_real(fr_plan p, const float *d_w, float *d_grid, void *stream)
 {
     if (!p || !d_grid || (p->n && !d_w)) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");

@@ -114,6 +114,74 @@ __global__ void __launch_bounds__(256) degrid_kernel(DegridParams P)
     }
 }
 
+// -- streaming acquisition: incremental regridding -----------------------------
+// The gridded change dcf * (new - old) of the samples [begin, begin + count)
+// added into the grid with global atomic adds: thread per (sample, block of
+// CB coils), the same cell range, LUT index and checkerboard signs as the
+// scatter and the degridding.
+struct UpdateParams {
+    DegridParams g;          // geometry, LUT, grid size, checkerboard flag
+    const float2 *old_k;     // channels x n: the k-space the grid was made from
+    const float2 *new_k;     // channels x count: the new values
+    const float *dcf;        // n
+    float2 *grid;            // channels x cells
+    long long begin, count;
+};
+
+template <int CB>
+__global__ void __launch_bounds__(256) grid_update_kernel(UpdateParams U)
+{
+    extern __shared__ float4 lutS[];
+    const DegridParams &P = U.g;
+    for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutS[i] = P.lut_e[i];
+    __syncthreads();
+    const int c0 = blockIdx.y * CB;
+    const size_t G = (size_t)P.G;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < U.count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long sidx = U.begin + i;
+        const float4 p = P.traj[sidx];
+        const float d = U.dcf[sidx];
+        float2 v[CB];
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            v[c] = make_float2(0.f, 0.f);
+            if (c0 + c < P.channels) {
+                const float2 a = U.new_k[(size_t)(c0 + c) * U.count + i];
+                const float2 b = U.old_k[(size_t)(c0 + c) * P.n + sidx];
+                v[c] = make_float2(__fmul_rn(d, __fsub_rn(a.x, b.x)), __fmul_rn(d, __fsub_rn(a.y, b.y)));
+            }
+        }
+        int xs, xe, ys, ye, zs = 0, ze = 0;
+        comp_range(p.x, P.hw, P.G, xs, xe);
+        comp_range(p.y, P.hw, P.G, ys, ye);
+        if (P.dim == 3) comp_range(p.z, P.hw, P.G, zs, ze);
+        for (int z = zs; z <= ze; ++z) {
+            const float dz = P.dim == 3 ? __fsub_rn((float)z, p.z) : 0.f;
+            const float dz2 = __fmul_rn(dz, dz);
+            for (int y = ys; y <= ye; ++y) {
+                const float dy = __fsub_rn((float)y, p.y);
+                const float dzy = __fadd_rn(dz2, __fmul_rn(dy, dy));
+                const size_t row = ((size_t)z * G + (size_t)y) * G;
+                for (int x = xs; x <= xe; ++x) {
+                    const float dx = __fsub_rn((float)x, p.x);
+                    float w;
+                    if (!lut_weight(__fadd_rn(dzy, __fmul_rn(dx, dx)), lutS, P.smax, P.kc, P.L, w)) continue;
+                    if (P.checkerboard && ((x + y + z) & 1)) w = -w;
+#pragma unroll
+                    for (int c = 0; c < CB; ++c) {
+                        if (c0 + c < P.channels) {
+                            float *g = reinterpret_cast<float *>(U.grid + (size_t)(c0 + c) * P.cells + row + x);
+                            atomicAdd(g, __fmul_rn(w, v[c].x));
+                            atomicAdd(g + 1, __fmul_rn(w, v[c].y));
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
 // -- real-valued tile scatter of per-sample weights ---------------------------
 struct RealGridParams {
     const float4 *traj;
@@ -299,6 +367,36 @@ int degrid_run(fr_plan p, const float *d_grid, int channels, float *d_out, cudaS
     dim3 grid(bx, (channels + CB - 1) / CB);
     degrid_kernel<CB><<<grid, 256, smem, s>>>(P);
     FR_CHECK_LAUNCH("degrid_kernel");
+    return FR_OK;
+}
+
+int grid_update_run(fr_plan p, float *d_kdata, const float *d_new, size_t begin, size_t count, const float *d_dcf,
+                    int channels, float *d_grid, cudaStream_t s)
+{
+    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "fr_grid_update called before fr_plan_set_trajectory");
+    if (channels <= 0) return fail(FR_ERR_INVALID_ARGUMENT, "channels must be positive");
+    if (begin > p->n || count > p->n - begin) return fail(FR_ERR_SIZE_MISMATCH, "sample range exceeds the plan's samples");
+    if (count == 0) return FR_OK;
+    UpdateParams U;
+    U.g = degrid_params(p);
+    U.g.channels = channels;
+    U.old_k = reinterpret_cast<const float2 *>(d_kdata);
+    U.new_k = reinterpret_cast<const float2 *>(d_new);
+    U.dcf = d_dcf;
+    U.grid = reinterpret_cast<float2 *>(d_grid);
+    U.begin = (long long)begin;
+    U.count = (long long)count;
+    constexpr int CB = 4;
+    const size_t smem = (size_t)U.g.L * 16;
+    if (smem > 48 * 1024)
+        FR_CUDA(cudaFuncSetAttribute(grid_update_kernel<CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int bx = (int)std::min<long long>(((long long)count + 255) / 256, (long long)sm_count() * 8);
+    dim3 grid(bx, (channels + CB - 1) / CB);
+    grid_update_kernel<CB><<<grid, 256, smem, s>>>(U);
+    FR_CHECK_LAUNCH("grid_update_kernel");
+    // then the k-space itself: row c of the new values into coil c at `begin`
+    FR_CUDA(cudaMemcpy2DAsync(d_kdata + 2 * begin, p->n * 8, d_new, count * 8, count * 8, (size_t)channels,
+                              cudaMemcpyDeviceToDevice, s));
     return FR_OK;
 }
 

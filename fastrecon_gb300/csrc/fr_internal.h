@@ -237,6 +237,8 @@ namespace fr {
 // Density compensation and degridding (fr_dcf.cu).
 int dcf_analytic_run(const float *d_traj, size_t n, int dim, float power, float *d_out, cudaStream_t s);
 int degrid_run(fr_plan p, const float *d_grid, int channels, float *d_out, cudaStream_t s);
+int grid_update_run(fr_plan p, float *d_kdata, const float *d_new, size_t begin, size_t count, const float *d_dcf,
+                    int channels, float *d_grid, cudaStream_t s);
 int grid_real_run(fr_plan p, const float *d_w, float *d_grid, cudaStream_t s);
 int dcf_pipe_run(fr_plan p, int iterations, float *d_w, cudaStream_t s);
 // Density features (fr_density.cu) and the DCF network (fr_mlp.cu).

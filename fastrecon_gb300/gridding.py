@@ -166,6 +166,19 @@ class GridPlan:
         check(self.lib.fr_degrid(self.h, _ptr(grid), ch, _ptr(out), C.c_void_p(_stream(stream))), "fr_degrid")
         return out
 
+    def update(self, kdata, new, begin: int, dcf, grid, stream=None):
+        """Streaming acquisition (fr_grid_update): replace samples [begin, begin + new.shape[1]) of
+        ``kdata`` (C, N) complex64 by ``new`` (C, count) and add the gridded change into ``grid``
+        (the output of ``grid(kdata, dcf)`` for this plan), both in place."""
+        torch = _torch()
+        assert kdata.dtype == torch.complex64 and kdata.is_cuda and kdata.is_contiguous()
+        assert grid.dtype == torch.complex64 and grid.is_cuda and grid.is_contiguous()
+        new = new.contiguous()
+        ch, count = new.shape
+        check(self.lib.fr_grid_update(self.h, _ptr(kdata), _ptr(new), begin, count, _ptr(dcf.contiguous()), ch,
+                                      _ptr(grid), C.c_void_p(_stream(stream))), "fr_grid_update")
+        return grid
+
     def grid_real(self, w, out=None, stream=None):
         """Real-valued gridding of per-sample weights: (N,) float32 -> (G^d,) float32."""
         torch = _torch()

@@ -234,6 +234,22 @@ int fr_dcf_analytic(const float *d_traj, size_t n, int dim, float power, float *
  * range and LUT index; a checkerboard plan reads the grid with the same
  * (-1)^(x+y+z) signs). */
 int fr_degrid(fr_plan plan, const float *d_grid, int channels, float *d_kdata, void *stream);
+/* Streaming acquisition: ReconData::updateSingleAcquisition on the device
+ * (ReconData.cpp:179-189, cuReconData.cu:52-62: copy one readout into each
+ * channel at offset samples * acquisition and patch the device copy) plus
+ * incremental regridding, so a grid made by fr_grid follows the data as
+ * readouts arrive or are replaced without regridding every sample.
+ * d_kdata: the channels x n complex64 k-space d_grid was made from (device,
+ * coil-major, n = the plan's samples); d_new: channels x count complex64 new
+ * values of samples [sample_begin, sample_begin + count) (one readout:
+ * sample_begin = samples * acquisition, count = samples); d_dcf: the n DCF
+ * values.  Adds dcf * (new - old) gridded with the plan's kernel (and its
+ * checkerboard signs) into d_grid with global atomic adds, then copies
+ * d_new into d_kdata.  d_grid then equals fr_grid of the updated k-space up
+ * to float rounding (the adds' order is not fixed).  FR_ERR_SIZE_MISMATCH
+ * when the range exceeds the plan's samples. */
+int fr_grid_update(fr_plan plan, float *d_kdata, const float *d_new, size_t sample_begin, size_t count,
+                   const float *d_dcf, int channels, float *d_grid, void *stream);
 /* Real-valued gridding of per-sample weights into G^d floats (no DCF). */
 int fr_grid_real(fr_plan plan, const float *d_w, float *d_grid, void *stream);
 /* Pipe-Menon iterative DCF (MRM 41:179, 1999): `iterations` times
