@@ -37,7 +37,7 @@ class ReconDesc(C.Structure):
     _fields_ = [("dim", C.c_int), ("recon_size", C.c_uint), ("overgrid_factor", C.c_float),
                 ("kernel_width", C.c_float), ("lut_length", C.c_int), ("out_size", C.c_uint * 3),
                 ("channels", C.c_int), ("max_samples", C.c_size_t), ("tile", C.c_int * 3), ("coil_group", C.c_int),
-                ("flags", C.c_uint)]
+                ("flags", C.c_uint), ("grid_budget", C.c_size_t)]
 
 
 _VP = C.c_void_p

@@ -31,6 +31,9 @@ namespace {
 
 constexpr int kMaxPasses = 12;
 constexpr int kMaxN = 1024;
+// SoS modes of the last stage (coils in slabs): continue the sum already in
+// the output, and apply sqrt (/ deapod) at the end
+constexpr int kSosAccIn = 1, kSosFinal = 2;
 
 struct FftPlan1D {
     int n;
@@ -262,6 +265,9 @@ __global__ void __launch_bounds__(256) fft_x_kernel(const float2 *__restrict__ i
 // input), keep outputs [y0, y0 + ry).  Input index: base(outer) + e*stride + c.
 // If `sos_out` is given this is the last stage: |X|^2 is summed over `coils`
 // consecutive inputs (coil stride `cstride`), then sqrt (/ deapod).
+// sos_mode (coils in slabs): kSosAccIn starts the sum from the value in
+// sos_out, kSosFinal applies sqrt (/ deapod); without kSosFinal the plain
+// sum is stored.
 constexpr int kCols = 16;
 
 __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__ in, float2 *__restrict__ out,
@@ -269,7 +275,7 @@ __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__
                                                       long long in_outer_stride, long long out_outer_stride,
                                                       long long out_stride, const float2 *__restrict__ tw_g,
                                                       int coils, long long cstride, float *__restrict__ sos_out,
-                                                      const float *__restrict__ deapod)
+                                                      const float *__restrict__ deapod, int sos_mode)
 {
     extern __shared__ float2 sm[];
     const int n = pl.n;
@@ -283,7 +289,10 @@ __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__
     const int c0 = (blockIdx.x % cblocks) * kCols;
     const int cw = min(kCols, ncols - c0);
     if (sos_out)
-        for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) acc[i] = 0.f;
+        for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) {
+            const int e = i / kCols, c = i - e * kCols;
+            acc[i] = (sos_mode & kSosAccIn) && c < cw ? sos_out[outer * out_outer_stride + c0 + e * out_stride + c] : 0.f;
+        }
     for (int coil = 0; coil < (sos_out ? coils : 1); ++coil) {
         const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
         __syncthreads();
@@ -316,8 +325,11 @@ __global__ void __launch_bounds__(256) fft_col_kernel(const float2 *__restrict__
         for (int i = threadIdx.x; i < ry * kCols; i += blockDim.x) {
             const int e = i / kCols, c = i - e * kCols;
             if (c < cw) {
-                float m = __fsqrt_rn(acc[i]);
-                if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                float m = acc[i];
+                if (sos_mode & kSosFinal) {
+                    m = __fsqrt_rn(m);
+                    if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                }
                 dst[e * out_stride + c] = m;
             }
         }
@@ -359,7 +371,7 @@ __global__ void __launch_bounds__(256) fft_col_kernel_ct(const float2 *__restric
                                                          long long in_outer_stride, long long out_outer_stride,
                                                          long long out_stride, const float2 *__restrict__ tw_g,
                                                          int coils, long long cstride, float *__restrict__ sos_out,
-                                                         const float *__restrict__ deapod)
+                                                         const float *__restrict__ deapod, int sos_mode)
 {
     extern __shared__ float2 sm[];
     constexpr int C = kColsCt;
@@ -373,7 +385,10 @@ __global__ void __launch_bounds__(256) fft_col_kernel_ct(const float2 *__restric
     const int c0 = (blockIdx.x % cblocks) * C;
     const int cw = min(C, ncols - c0);
     if (sos_out)
-        for (int i = threadIdx.x; i < ry * C; i += blockDim.x) acc[i] = 0.f;
+        for (int i = threadIdx.x; i < ry * C; i += blockDim.x) {
+            const int e = i / C, c = i - e * C;
+            acc[i] = (sos_mode & kSosAccIn) && c < cw ? sos_out[outer * out_outer_stride + c0 + e * out_stride + c] : 0.f;
+        }
     for (int coil = 0; coil < (sos_out ? coils : 1); ++coil) {
         const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
         __syncthreads();
@@ -405,8 +420,11 @@ __global__ void __launch_bounds__(256) fft_col_kernel_ct(const float2 *__restric
         for (int i = threadIdx.x; i < ry * C; i += blockDim.x) {
             const int e = i / C, c = i - e * C;
             if (c < cw) {
-                float m = __fsqrt_rn(acc[i]);
-                if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                float m = acc[i];
+                if (sos_mode & kSosFinal) {
+                    m = __fsqrt_rn(m);
+                    if (dp) m = __fdiv_rn(m, dp[e * out_stride + c]);
+                }
                 dst[e * out_stride + c] = m;
             }
         }
@@ -415,7 +433,7 @@ __global__ void __launch_bounds__(256) fft_col_kernel_ct(const float2 *__restric
 
 using FftXFn = void (*)(const float2 *, float2 *, long long, int, int, const float2 *);
 using FftColFn = void (*)(const float2 *, float2 *, int, int, int, long long, long long, long long, long long,
-                          const float2 *, int, long long, float *, const float *);
+                          const float2 *, int, long long, float *, const float *, int);
 struct CtKernels {
     int n;
     FftXFn x;
@@ -575,12 +593,16 @@ int fr_fft_crop_sos_destroy(fr_fftcs f)
     return FR_OK;
 }
 
-int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deapod, float *d_out, void *stream)
+}  // extern "C"
+
+namespace fr {
+// The pruned transform of `channels` <= the object's coils; sos_mode as in
+// the column kernels (kSosFinal alone: the whole SoS of these coils).
+int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_deapod, float *d_out, int sos_mode,
+                  cudaStream_t s)
 {
-    if (!f || !d_grid || !d_out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
-    cudaStream_t s = (cudaStream_t)stream;
     const int G = (int)f->G;
-    const int C = f->channels;
+    const int C = channels;
     const int rx = f->out[0], ry = f->out[1], rz = f->out[2];
     const int x0 = (G - rx) / 2, y0 = (G - ry) / 2, z0 = (G - rz) / 2;
     const float2 *tw = f->tw.as<float2>();
@@ -602,17 +624,17 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
         const int cb = (rx + kRegCols - 1) / kRegCols;
         if (f->dim == 2) {
             rk->col_sos<<<cb, rk->colthreads, rk->colsmem, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C,
-                                                            (long long)G * rx, d_out, d_deapod);
+                                                            (long long)G * rx, d_out, d_deapod, sos_mode);
             FR_CHECK_LAUNCH("fft_col_kernel_reg(y, sos)");
             return FR_OK;
         }
         float2 *b2 = f->b2.as<float2>();
         rk->col<<<(unsigned)((long long)C * G * cb), rk->colthreads, rk->colsmem, s>>>(
-            b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+            b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(y)");
         rk->col_sos<<<(unsigned)((long long)ry * cb), rk->colthreads, rk->colsmem, s>>>(
             b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C, (long long)G * ry * rx, d_out,
-            d_deapod);
+            d_deapod, sos_mode);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(z, sos)");
         return FR_OK;
     }
@@ -631,11 +653,11 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
         // y stage: input bx[c][z][y][x], columns x0..x0+rx, element (y) stride G
         ck->col<<<(unsigned)((long long)C * G * cb), 256, smc, s>>>(f->bx.as<float2>() + x0, b2, y0, ry, rx, G,
                                                                    (long long)G * G, (long long)ry * rx, rx, tw, 1, 0,
-                                                                   nullptr, nullptr);
+                                                                   nullptr, nullptr, 0);
         FR_CHECK_LAUNCH("fft_col_kernel_ct(y)");
         ck->col<<<(unsigned)((long long)ry * cb), 256, smc, s>>>(b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx,
                                                                 (long long)ry * rx, tw, C, (long long)G * ry * rx,
-                                                                d_out, d_deapod);
+                                                                d_out, d_deapod, sos_mode);
         FR_CHECK_LAUNCH("fft_col_kernel_ct(z, sos)");
         return FR_OK;
     }
@@ -651,17 +673,17 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
         const int cb = (rx + kColsCt - 1) / kColsCt;
         if (f->dim == 2) {
             ck->col<<<cb, 256, smc, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C, (long long)G * rx, d_out,
-                                         d_deapod);
+                                         d_deapod, sos_mode);
             FR_CHECK_LAUNCH("fft_col_kernel_ct(y, sos)");
             return FR_OK;
         }
         float2 *b2 = f->b2.as<float2>();
         ck->col<<<(unsigned)((long long)C * G * cb), 256, smc, s>>>(b1, b2, y0, ry, rx, rx, (long long)G * rx,
-                                                                   (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+                                                                   (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0);
         FR_CHECK_LAUNCH("fft_col_kernel_ct(y)");
         ck->col<<<(unsigned)((long long)ry * cb), 256, smc, s>>>(b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx,
                                                                 (long long)ry * rx, tw, C, (long long)G * ry * rx,
-                                                                d_out, d_deapod);
+                                                                d_out, d_deapod, sos_mode);
         FR_CHECK_LAUNCH("fft_col_kernel_ct(z, sos)");
         return FR_OK;
     }
@@ -680,22 +702,31 @@ int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deap
         // y stage + SoS: outer = nothing (one plane), columns = x'
         // input b1[c][y][x'] : element stride rx, coil stride G*rx
         fft_col_kernel<<<cblocks, 256, smc, s>>>(b1, nullptr, f->pl, y0, ry, rx, rx, 0, 0, rx, tw, C,
-                                                 (long long)G * rx, d_out, d_deapod);
+                                                 (long long)G * rx, d_out, d_deapod, sos_mode);
         FR_CHECK_LAUNCH("fft_col_kernel(y, sos)");
         return FR_OK;
     }
     // y stage: outer = (c, z), columns = x', input b1[c][z][y][x']
     float2 *b2 = f->b2.as<float2>();
     fft_col_kernel<<<(unsigned)((long long)C * G * cblocks), 256, smc, s>>>(
-        b1, b2, f->pl, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr);
+        b1, b2, f->pl, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0);
     FR_CHECK_LAUNCH("fft_col_kernel(y)");
     // z stage + SoS: outer = y', columns = x', input b2[c][z][y'][x'] with
     // element (z) stride ry*rx, coil stride G*ry*rx; output out[z'][y'][x']
     fft_col_kernel<<<(unsigned)((long long)ry * cblocks), 256, smc, s>>>(
         b2, nullptr, f->pl, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C,
-        (long long)G * ry * rx, d_out, d_deapod);
+        (long long)G * ry * rx, d_out, d_deapod, sos_mode);
     FR_CHECK_LAUNCH("fft_col_kernel(z, sos)");
     return FR_OK;
+}
+}  // namespace fr
+
+extern "C" {
+
+int fr_fft_crop_sos_execute(fr_fftcs f, const float *d_grid, const float *d_deapod, float *d_out, void *stream)
+{
+    if (!f || !d_grid || !d_out) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    return fftcs_execute(f, d_grid, f->channels, d_deapod, d_out, kSosFinal, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -200,7 +200,7 @@ template <int N, bool SOS>
 __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) fft_col_kernel_reg(
     const float2 *__restrict__ in, float2 *__restrict__ out, int y0, int ry, int ncols, long long stride,
     long long in_outer_stride, long long out_outer_stride, long long out_stride, const float2 *__restrict__ tw_g,
-    int coils, long long cstride, float *__restrict__ sos_out, const float *__restrict__ deapod)
+    int coils, long long cstride, float *__restrict__ sos_out, const float *__restrict__ deapod, int sos_mode)
 {
     constexpr int T = RegSplit<N>::T, M = RegSplit<N>::M;
     constexpr int CB = kRegCols;
@@ -216,6 +216,16 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
     float acc[SOS ? T : 1];
 #pragma unroll
     for (int k2 = 0; k2 < (SOS ? T : 1); ++k2) acc[k2] = 0.f;
+    if (SOS && (sos_mode & kSosAccIn) && threadIdx.x < CB * M && col_ok) {
+        // coils in slabs: continue the previous slabs' sum
+        const int k1 = threadIdx.x / CB;
+        const float *o = sos_out + outer * out_outer_stride + c0 + col;
+#pragma unroll
+        for (int k2 = 0; k2 < T; ++k2) {
+            const int k = k1 + M * k2;
+            if (k >= y0 && k < y0 + ry) acc[k2] = o[(long long)(k - y0) * out_stride];
+        }
+    }
     const int ncoil = SOS ? coils : 1;
     for (int coil = 0; coil < ncoil; ++coil) {
         __syncthreads();  // twiddles staged; the previous coil's exchange is read
@@ -262,8 +272,11 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
         for (int k2 = 0; k2 < T; ++k2) {
             const int k = k1 + M * k2;
             if (k >= y0 && k < y0 + ry) {
-                float m = __fsqrt_rn(acc[k2]);
-                if (dp) m = __fdiv_rn(m, dp[(long long)(k - y0) * out_stride]);
+                float m = acc[k2];
+                if (sos_mode & kSosFinal) {
+                    m = __fsqrt_rn(m);
+                    if (dp) m = __fdiv_rn(m, dp[(long long)(k - y0) * out_stride]);
+                }
                 o[(long long)(k - y0) * out_stride] = m;
             }
         }

@@ -16,8 +16,10 @@ struct Size3 {
     unsigned x, y, z;
 };
 
+// sos_mode bit 1: continue the sum already in `out` (coils in slabs);
+// bit 2: apply sqrt (/ deapod), else store the plain sum.
 __global__ void sos_kernel(const float2 *__restrict__ imgs, int channels, Size3 in, Size3 rec,
-                           Size3 off, const float *__restrict__ deapod, float *__restrict__ out)
+                           Size3 off, const float *__restrict__ deapod, float *__restrict__ out, int sos_mode)
 {
     const size_t nout = (size_t)rec.x * rec.y * rec.z;
     const size_t cells = (size_t)in.x * in.y * in.z;
@@ -28,15 +30,18 @@ __global__ void sos_kernel(const float2 *__restrict__ imgs, int channels, Size3 
         unsigned y = (unsigned)(r % rec.y);
         unsigned z = (unsigned)(r / rec.y);
         size_t in_idx = ((size_t)(z + off.z) * in.y + (y + off.y)) * in.x + (x + off.x);
-        float acc = 0.f;
+        float acc = (sos_mode & 1) ? out[o] : 0.f;
         for (int c = 0; c < channels; ++c) {
             float2 v = imgs[(size_t)c * cells + in_idx];
             // std::complex<float>: x * conj(x) real part = a*a - b*(-b)
             float re = __fsub_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, -v.y));
             acc = __fadd_rn(acc, re);
         }
-        float m = __fsqrt_rn(acc);
-        if (deapod) m = __fdiv_rn(m, deapod[o]);
+        float m = acc;
+        if (sos_mode & 2) {
+            m = __fsqrt_rn(m);
+            if (deapod) m = __fdiv_rn(m, deapod[o]);
+        }
         out[o] = m;
     }
 }
@@ -160,14 +165,14 @@ int check_crop(int dim, const unsigned *size, const unsigned *rec, Size3 &in, Si
 }  // namespace
 
 int sos_run(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *recon,
-            const float *d_deapod, float *d_out, cudaStream_t s)
+            const float *d_deapod, float *d_out, cudaStream_t s, int sos_mode)
 {
     Size3 in, r, off;
     int st = check_crop(dim, size, recon, in, r, off);
     if (st) return st;
     size_t nout = (size_t)r.x * r.y * r.z;
     sos_kernel<<<blocks_for(nout, 256), 256, 0, s>>>(reinterpret_cast<const float2 *>(d_imgs), channels, in, r,
-                                                     off, d_deapod, d_out);
+                                                     off, d_deapod, d_out, sos_mode);
     FR_CHECK_LAUNCH("sos_kernel");
     return FR_OK;
 }

@@ -122,8 +122,10 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
              cudaStream_t s);
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
+// sos_mode: 2 = the whole SoS (sqrt, / deapod); for coils in slabs 0 = store
+// the plain sum of |x|^2, | 1 = add to the sum already in d_out.
 int sos_run(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *recon,
-            const float *d_deapod, float *d_out, cudaStream_t s);
+            const float *d_deapod, float *d_out, cudaStream_t s, int sos_mode = 2);
 int shift_run(float *d_imgs, int channels, int dim, const unsigned *size, cudaStream_t s);
 int crop_run(const float *d_imgs, int channels, int dim, const unsigned *size, const unsigned *crop,
              float *d_out, cudaStream_t s);
@@ -258,6 +260,10 @@ int to_bf16_run(const float *d_a, void *d_b, int count, cudaStream_t s);
 namespace fr {
 // True when the pruned FFT has compile-time specialised passes for G.
 bool pruned_fft_specialised(int G);
+// The pruned transform + crop + SoS of `channels` (<= the object's) coils;
+// sos_mode as sos_run's.
+int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_deapod, float *d_out, int sos_mode,
+                  cudaStream_t s);
 }  // namespace fr
 
 namespace fr {

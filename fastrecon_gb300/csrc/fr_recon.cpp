@@ -8,6 +8,7 @@
 // FFT output is already shifted and no extra pass over the grid is needed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <new>
 
@@ -19,6 +20,7 @@ struct fr_recon_s {
     fr_recon_desc d;
     unsigned G = 0;
     size_t cells = 0;
+    int slab = 0;            // coils gridded and transformed together (grid_budget)
     bool checkerboard = false;
     std::vector<float> lut;
     fr_plan plan = nullptr;
@@ -66,6 +68,11 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     r->G = (unsigned)((float)d->recon_size * d->overgrid_factor);
     r->cells = d->dim == 3 ? (size_t)r->G * r->G * r->G : (size_t)r->G * r->G;
     r->checkerboard = (r->G % 2) == 0;
+    r->slab = d->channels;
+    if (d->grid_budget > 0) {
+        const size_t per = r->cells * 8;
+        r->slab = (int)std::max<size_t>(1, std::min<size_t>((size_t)d->channels, d->grid_budget / per));
+    }
     r->lut.resize(d->lut_length > 1 ? d->lut_length : 2);
     int st = fr_kb_lut(d->kernel_width, d->overgrid_factor, d->lut_length, r->lut.data());
     if (st) {
@@ -92,14 +99,14 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     const bool want_pruned = (d->flags & FR_RECON_PRUNED_FFT) || pruned_fft_specialised((int)r->G);
     if (!st && r->checkerboard && want_pruned && !(d->flags & FR_RECON_CUFFT)) {
         // the pruned transform where the grid size factors into 2, 3, 5
-        if (fr_fft_crop_sos_create(d->dim, r->G, d->channels, r->d.out_size, &r->pruned) != FR_OK)
+        if (fr_fft_crop_sos_create(d->dim, r->G, r->slab, r->d.out_size, &r->pruned) != FR_OK)
             r->pruned = nullptr;
     }
     if (!st && !r->pruned) {
         unsigned sz[3] = {r->G, r->G, d->dim == 3 ? r->G : 1u};
-        st = fr_fft_create(d->dim, sz, d->channels, +1, &r->fft);
+        st = fr_fft_create(d->dim, sz, r->slab, +1, &r->fft);
     }
-    if (!st && r->grid.reserve(r->cells * 8 * (size_t)d->channels)) st = FR_ERR_OUT_OF_MEMORY;
+    if (!st && r->grid.reserve(r->cells * 8 * (size_t)r->slab)) st = FR_ERR_OUT_OF_MEMORY;
     if (st) {
         delete r;
         return st;
@@ -162,19 +169,29 @@ int recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *
         cudaError_t e = cudaStreamWaitEvent(s, kdata_ready, 0);
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
     }
-    if (!st) st = fr_grid(r->plan, d_kdata, d_dcf, r->d.channels, g, stream);
-    if (r->timing) cudaEventRecord(r->ev[2], s);
     const float *deapod = (r->d.flags & FR_RECON_DEAPODIZE) ? r->deapod.as<float>() : nullptr;
-    if (r->pruned) {
-        // transform, crop and SoS in one pruned pass (the stage times are
-        // reported as fft, with sos 0)
-        if (!st) st = fr_fft_crop_sos_execute(r->pruned, g, deapod, d_image, stream);
-        if (r->timing) cudaEventRecord(r->ev[3], s);
-    } else {
-        if (!st) st = fr_fft_execute(r->fft, g, stream);
-        if (!st && !r->checkerboard) st = shift_run(g, r->d.channels, r->d.dim, sz, s);
-        if (r->timing) cudaEventRecord(r->ev[3], s);
-        if (!st) st = sos_run(g, r->d.channels, r->d.dim, sz, r->d.out_size, deapod, d_image, s);
+    // coils in slabs of r->slab (all at once unless grid_budget asks for
+    // less): the first slab stores its sum of |x|^2, later slabs add to it in
+    // coil order, the last applies sqrt (/ deapod).  With several slabs the
+    // stage times are those of the first slab's gridding and of everything
+    // after it.
+    const int C = r->d.channels;
+    for (int c0 = 0; !st && c0 < C; c0 += r->slab) {
+        const int cs = std::min(r->slab, C - c0);
+        const int mode = (c0 > 0 ? 1 : 0) | (c0 + cs == C ? 2 : 0);
+        st = fr_grid(r->plan, d_kdata + 2 * (size_t)c0 * n, d_dcf, cs, g, stream);
+        if (r->timing && c0 == 0) cudaEventRecord(r->ev[2], s);
+        if (r->pruned) {
+            // transform, crop and SoS in one pruned pass (the stage times are
+            // reported as fft, with sos 0)
+            if (!st) st = fftcs_execute(r->pruned, g, cs, deapod, d_image, mode, s);
+            if (r->timing && c0 + cs == C) cudaEventRecord(r->ev[3], s);
+        } else {
+            if (!st) st = fr_fft_execute(r->fft, g, stream);
+            if (!st && !r->checkerboard) st = shift_run(g, cs, r->d.dim, sz, s);
+            if (r->timing && c0 + cs == C) cudaEventRecord(r->ev[3], s);
+            if (!st) st = sos_run(g, cs, r->d.dim, sz, r->d.out_size, deapod, d_image, s, mode);
+        }
     }
     if (r->timing) {
         cudaEventRecord(r->ev[4], s);

@@ -318,7 +318,8 @@ class Recon:
 
     def __init__(self, dim: int, recon_size: int, overgrid_factor: float, channels: int, out_size=None,
                  kernel_width: float = 4.0, lut_length: int = 512, max_samples: int = 0, tile=(0, 0, 0),
-                 coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False, pruned_fft: bool = False):
+                 coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False, pruned_fft: bool = False,
+                 grid_budget: int = 0):
         self.lib = capi.load()
         d = capi.ReconDesc()
         d.dim = dim
@@ -336,6 +337,7 @@ class Recon:
         d.coil_group = coil_group
         d.flags = ((capi.FR_RECON_DEAPODIZE if deapodize else 0) | (capi.FR_RECON_CUFFT if use_cufft else 0) |
                    (capi.FR_RECON_PRUNED_FFT if pruned_fft else 0))
+        d.grid_budget = grid_budget  # bytes of grid workspace: coils in slabs (0: all at once)
         h = C.c_void_p()
         check(self.lib.fr_recon_create(C.byref(d), C.byref(h)), "fr_recon_create")
         self.h = h

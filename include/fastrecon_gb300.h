@@ -383,6 +383,13 @@ typedef struct {
     int tile[3];             /* 0 = default */
     int coil_group;          /* 0 = default */
     unsigned flags;          /* FR_RECON_* */
+    size_t grid_budget;      /* out-of-core coils (cuGridLut's partitions, cuGridLut.cu:128-149,182-220,
+                                bound the memory of its pair map; here the grid is the large buffer):
+                                0 = grid all coils at once; else coils are gridded and transformed in
+                                slabs whose complex grid fits grid_budget bytes (at least one coil per
+                                slab), the |x|^2 of each slab added to the image in coil order, so the
+                                image equals the single-slab one while the grid workspace shrinks from
+                                channels x G^d x 8 to slab x G^d x 8 bytes */
 } fr_recon_desc;
 
 int fr_recon_create(const fr_recon_desc *desc, fr_recon *out);

@@ -1,0 +1,61 @@
+"""Out-of-core coils (fr_recon_desc.grid_budget): the grid workspace holds a
+slab of coils at a time; each slab's |x|^2 is added to the image in coil
+order, so the image must equal the one made with every coil at once."""
+import numpy as np
+import pytest
+
+from conftest import load_case, rel_l2
+
+
+def _run(torch, c, budget, **kw):
+    import fastrecon_gb300 as fr
+    r = fr.Recon(c["dim"], c["recon"], c["os"], c["coils"], kernel_width=c["W"], lut_length=c["L"],
+                 grid_budget=budget, **kw)
+    img = r.run(torch.from_numpy(c["traj"]).cuda(), torch.from_numpy(c["dcf"]).cuda(),
+                torch.from_numpy(c["kdata"]).cuda())
+    return img.cpu().numpy()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small", "radial2d_oddgrid"])
+@pytest.mark.parametrize("mode", [dict(), dict(use_cufft=True), dict(deapodize=True), dict(pruned_fft=True)])
+def test_slabs_equal_single_pass(name, mode):
+    import torch
+    c = load_case(name)
+    if c["coils"] < 2:
+        pytest.skip("one coil")
+    cells = c["G"] ** c["dim"]
+    whole = _run(torch, c, 0, **mode)
+    for coils_per_slab in (1, 2, c["coils"] - 1):
+        got = _run(torch, c, coils_per_slab * cells * 8 + 7, **mode)
+        assert rel_l2(got, whole) <= 1e-6, coils_per_slab
+    # the reference image itself (parity bar of the recon tests)
+    if not mode:
+        assert rel_l2(_run(torch, c, cells * 8, **mode), c["image"]) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_slab_budget_smaller_than_one_coil_still_runs():
+    import torch
+    c = load_case("radial2d_small")
+    whole = _run(torch, c, 0)
+    assert rel_l2(_run(torch, c, 1), whole) <= 1e-6  # at least one coil per slab
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("coils_per_slab", [1, 3, 4])
+def test_slabs_3d_register_fft(coils_per_slab):
+    """A 3D grid size with the register FFT stages (64^3), 5 coils."""
+    import torch
+
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import synth
+    t = synth.kooshball_3d(300, 64)
+    kd = synth.kspace(t, 3, 32, 5, seed=3, xp=torch, device="cuda")
+    td = torch.from_numpy(t).cuda()
+    dcf = fr.dcf_analytic(td, 3, 2.0)
+    imgs = []
+    for budget in (0, coils_per_slab * 64 ** 3 * 8):
+        r = fr.Recon(3, 32, 2.0, 5, grid_budget=budget, deapodize=True)
+        imgs.append(r.run(td, dcf, kd).cpu().numpy())
+    assert rel_l2(imgs[1], imgs[0]) <= 1e-6
