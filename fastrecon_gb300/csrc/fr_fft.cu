@@ -458,9 +458,10 @@ const CtKernels *ct_kernels(int n)
 }
 
 // Register two-step stages (fr_fft_reg.cuh) for the specialised sizes.
+using FftXRegFn = void (*)(const float2 *, float2 *, long long, int, int, const float2 *, XMask);
 struct RegKernels {
     int n;
-    FftXFn x;
+    FftXRegFn x;
     FftColFn col, col_sos;
     size_t xsmem, colsmem;
     int xthreads, colthreads;
@@ -598,8 +599,10 @@ int fr_fft_crop_sos_destroy(fr_fftcs f)
 namespace fr {
 // The pruned transform of `channels` <= the object's coils; sos_mode as in
 // the column kernels (kSosFinal alone: the whole SoS of these coils).
+bool fftcs_masks_tiles(fr_fftcs f) { return f && f->reg != nullptr; }
+
 int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_deapod, float *d_out, int sos_mode,
-                  cudaStream_t s)
+                  cudaStream_t s, const TileMask *tiles)
 {
     const int G = (int)f->G;
     const int C = channels;
@@ -619,7 +622,16 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
             FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
             FR_CUDA(cudaFuncSetAttribute(rk->col_sos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
         }
-        rk->x<<<(unsigned)((nl + kRegLinesX - 1) / kRegLinesX), rk->xthreads, rk->xsmem, s>>>(grid, b1, nl, x0, rx, tw);
+        XMask xm{};
+        if (tiles && tiles->bits) {
+            auto lg = [](int v) { return (v & (v - 1)) == 0 ? __builtin_ctz((unsigned)v) : -1; };
+            xm = XMask{tiles->bits, lg(tiles->tile[0]), lg(tiles->tile[1]), lg(tiles->tile[2]), tiles->ntile[0],
+                       tiles->ntile[1], G, (int)Gz};
+            if (xm.sx < 0 || xm.sy < 0 || xm.sz < 0)
+                return fail(FR_ERR_UNSUPPORTED, "tile masks need power-of-two tile edges");
+        }
+        rk->x<<<(unsigned)((nl + kRegLinesX - 1) / kRegLinesX), rk->xthreads, rk->xsmem, s>>>(grid, b1, nl, x0, rx, tw,
+                                                                                          xm);
         FR_CHECK_LAUNCH("fft_x_kernel_reg");
         const int cb = (rx + kRegCols - 1) / kRegCols;
         if (f->dim == 2) {

@@ -136,12 +136,20 @@ struct RegSplit {
 constexpr int kRegLinesX = 8;  // lines per CTA of the register x stage
 constexpr int kRegCols = 16;   // columns per CTA of the register column stages (128-byte rows)
 
+// Cells the gridding left unwritten (tiles without samples) read as zero:
+// bit ((z >> sz) * nty + (y >> sy)) * ntx + (x >> sx) of `bits` is set for
+// written tiles (power-of-two tile edges; bits == nullptr: every cell).
+struct XMask {
+    const unsigned *bits;
+    int sx, sy, sz, ntx, nty, G, Gz;
+};
+
 // x stage: kRegLinesX contiguous lines of length N per CTA, outputs
 // [x0, x0 + rx) of each line.  in: nlines x N, out: nlines x rx.
 template <int N>
 __global__ void __launch_bounds__(kRegLinesX * RegSplit<N>::TH) fft_x_kernel_reg(
     const float2 *__restrict__ in, float2 *__restrict__ out, long long nlines, int x0, int rx,
-    const float2 *__restrict__ tw_g)
+    const float2 *__restrict__ tw_g, XMask xm)
 {
     constexpr int T = RegSplit<N>::T, M = RegSplit<N>::M;
     constexpr int LS = M * (T + 1);  // [k1][t] with one pad slot per row
@@ -155,7 +163,16 @@ __global__ void __launch_bounds__(kRegLinesX * RegSplit<N>::TH) fft_x_kernel_reg
         const int l = threadIdx.x / T, t = threadIdx.x % T;
         const long long line = l0 + l;
         float2 v[M];
-        if (line < nlines) {
+        if (line < nlines && xm.bits) {
+            const int y = (int)(line % xm.G), z = (int)((line / xm.G) % xm.Gz);
+            const int tb = ((z >> xm.sz) * xm.nty + (y >> xm.sy)) * xm.ntx;
+            const float2 *src = in + line * N + t;
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int tile = tb + ((t + T * m) >> xm.sx);
+                v[m] = (xm.bits[tile >> 5] >> (tile & 31)) & 1u ? src[T * m] : make_float2(0.f, 0.f);
+            }
+        } else if (line < nlines) {
             const float2 *src = in + line * N + t;
 #pragma unroll
             for (int m = 0; m < M; ++m) v[m] = src[T * m];

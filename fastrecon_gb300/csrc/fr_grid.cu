@@ -56,6 +56,7 @@ struct GridParams {
     // a record's coil values are one contiguous run instead of one value per
     // coil plane
     int sample_major;
+    int skip_empty;     // tiles without samples are left unwritten
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -391,8 +392,8 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     unsigned *bmax_s = reinterpret_cast<unsigned *>(bsum_s + 64);
     float *inv_s = bsum_s + 128;
 
-    if (it.count == 0) {  // empty tile: stream zeros
-        write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, true, inv_s);
+    if (it.count == 0) {  // empty tile: stream zeros, unless the reader masks it
+        if (!P.skip_empty) write_cell_group<R>(P, gridf, acc, cg, ox, oy, oz, true, inv_s);
         return;
     }
 
@@ -730,7 +731,7 @@ void default_tiling(int dim, int *tile, int *coil_group, int channels)
 }
 
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
-             cudaStream_t s)
+             cudaStream_t s, bool skip_empty)
 {
     if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "fr_grid called before fr_plan_set_trajectory");
     if (channels <= 0) return fail(FR_ERR_INVALID_ARGUMENT, "channels must be positive");
@@ -767,6 +768,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.work_counter = nullptr;
     P.nwork = 0;
     P.sample_major = 0;
+    P.skip_empty = skip_empty ? 1 : 0;
     const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
     if (p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024) {
         if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2))) return FR_ERR_OUT_OF_MEMORY;
@@ -869,6 +871,7 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.work_counter = nullptr;
     P.nwork = 0;
     P.sample_major = 0;
+    P.skip_empty = 0;
     if (gi.nitems == 0) return FR_OK;
     if (gi.dim == 3) {
         switch (R) {
@@ -982,6 +985,7 @@ int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf,
     P.work_counter = b.work_counter;
     P.nwork = b.nitems * P.ngroups;
     P.sample_major = 0;
+    P.skip_empty = 0;
     if (P.nwork == 0) return FR_OK;
     if (P.nwork > 0x7FFFFFFFll) return fail(FR_ERR_UNSUPPORTED, "too many work items");
     if (b.dim == 3) {

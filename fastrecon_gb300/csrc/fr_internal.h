@@ -107,6 +107,7 @@ struct fr_plan_s {
     fr::DevBuf density_sat;   // G^d ints: per-cell counts -> summed-area table
     fr::DevBuf small;         // 256 bytes of scratch (feature max |k|)
     fr::DevBuf kt;            // n x channels complex: sample-major copy of the k-space (fr_grid)
+    fr::DevBuf tile_mask;     // ntiles bits: tile holds bin records (recon path skips the others)
     bool kspace_sample_major = true;  // cleared by FR_KSPACE_COIL_MAJOR=1
 
     // scatter-kernel timing (fr_plan_profile)
@@ -119,8 +120,10 @@ struct fr_plan_s {
 namespace fr {
 // Kernel-side entry points implemented in the .cu files.
 int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
+// skip_empty: leave the cells of tiles without samples unwritten (the
+// caller's next reader masks them with the plan's tile bitmap).
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
-             cudaStream_t s);
+             cudaStream_t s, bool skip_empty = false);
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
 // sos_mode: 2 = the whole SoS (sqrt, / deapod); for coils in slabs 0 = store
 // the plain sum of |x|^2, | 1 = add to the sum already in d_out.
@@ -262,8 +265,16 @@ namespace fr {
 bool pruned_fft_specialised(int G);
 // The pruned transform + crop + SoS of `channels` (<= the object's) coils;
 // sos_mode as sos_run's.
+// tiles (optional): the grid's unwritten tiles, as the plan's occupancy
+// bitmap over tiles of edge tile[0..2]; cells of empty tiles read as zero.
+struct TileMask {
+    const unsigned *bits = nullptr;
+    int tile[3] = {1, 1, 1};
+    int ntile[3] = {1, 1, 1};
+};
 int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_deapod, float *d_out, int sos_mode,
-                  cudaStream_t s);
+                  cudaStream_t s, const TileMask *tiles = nullptr);
+bool fftcs_masks_tiles(fr_fftcs f);  // the x stage takes a TileMask (register stages)
 }  // namespace fr
 
 namespace fr {

@@ -490,6 +490,20 @@ __global__ void items_kernel(const int *__restrict__ cnt, const TileScan *__rest
     }
 }
 
+// Bit t of the occupancy bitmap: tile t holds at least one bin record.
+__global__ void tile_mask_kernel(const int *__restrict__ cnt, long long ntiles, unsigned *__restrict__ mask)
+{
+    const long long nw = (ntiles + 31) / 32;
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nw; w += (long long)gridDim.x * blockDim.x) {
+        unsigned m = 0;
+        for (int b = 0; b < 32; ++b) {
+            const long long t = w * 32 + b;
+            if (t < ntiles && cnt[t] > 0) m |= 1u << b;
+        }
+        mask[w] = m;
+    }
+}
+
 __global__ void ranges_kernel(const float4 *__restrict__ traj, size_t n, int dim, unsigned G, float hw,
                               int *__restrict__ start, int *__restrict__ end)
 {
@@ -608,6 +622,10 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
                                                              p->chunk, p->items.as<WorkItem>(),
                                                              p->splits.as<SplitTile>());
     FR_CHECK_LAUNCH("items_kernel");
+    if (p->tile_mask.reserve((size_t)((p->ntiles + 31) / 32) * 4)) return FR_ERR_OUT_OF_MEMORY;
+    tile_mask_kernel<<<grid_blocks((p->ntiles + 31) / 32, 256), 256, 0, s>>>(p->tile_count.as<int>(), p->ntiles,
+                                                                              p->tile_mask.as<unsigned>());
+    FR_CHECK_LAUNCH("tile_mask_kernel");
     p->planned = true;
     return FR_OK;
 }

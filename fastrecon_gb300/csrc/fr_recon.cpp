@@ -175,16 +175,31 @@ int recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *
     // coil order, the last applies sqrt (/ deapod).  With several slabs the
     // stage times are those of the first slab's gridding and of everything
     // after it.
+    // The register FFT stages read the grid through the plan's tile bitmap,
+    // so the scatter leaves tiles without samples unwritten (for the
+    // kooshball about half the 384^3 grid: its corners).
+    TileMask tm;
+    const fr_plan p = r->plan;
+    const bool pow2 = ((p->tile[0] | p->tile[1] | p->tile[2]) > 0) && !(p->tile[0] & (p->tile[0] - 1)) &&
+                      !(p->tile[1] & (p->tile[1] - 1)) && !(p->tile[2] & (p->tile[2] - 1));
+    const bool skip = r->pruned && fftcs_masks_tiles(r->pruned) && pow2;
+    if (skip) {
+        tm.bits = p->tile_mask.as<unsigned>();
+        for (int i = 0; i < 3; ++i) {
+            tm.tile[i] = p->tile[i];
+            tm.ntile[i] = p->ntile[i];
+        }
+    }
     const int C = r->d.channels;
     for (int c0 = 0; !st && c0 < C; c0 += r->slab) {
         const int cs = std::min(r->slab, C - c0);
         const int mode = (c0 > 0 ? 1 : 0) | (c0 + cs == C ? 2 : 0);
-        st = fr_grid(r->plan, d_kdata + 2 * (size_t)c0 * n, d_dcf, cs, g, stream);
+        st = grid_run(r->plan, d_kdata + 2 * (size_t)c0 * n, d_dcf, cs, g, s, skip);
         if (r->timing && c0 == 0) cudaEventRecord(r->ev[2], s);
         if (r->pruned) {
             // transform, crop and SoS in one pruned pass (the stage times are
             // reported as fft, with sos 0)
-            if (!st) st = fftcs_execute(r->pruned, g, cs, deapod, d_image, mode, s);
+            if (!st) st = fftcs_execute(r->pruned, g, cs, deapod, d_image, mode, s, skip ? &tm : nullptr);
             if (r->timing && c0 + cs == C) cudaEventRecord(r->ev[3], s);
         } else {
             if (!st) st = fr_fft_execute(r->fft, g, stream);
