@@ -786,20 +786,23 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
         if (p->partials.reserve(bytes)) return FR_ERR_OUT_OF_MEMORY;
     }
     P.partials = p->partials.as<float>();
-    if (p->nitems == 0) return FR_OK;
+    // with skip_empty only the occupied tiles' items (the empty tiles'
+    // zero-fill items are last in the list)
+    const long long nlaunch = skip_empty ? p->nitems_occupied : p->nitems;
+    if (nlaunch == 0) return FR_OK;
     if (p->dim == 3) {
         switch (R) {
-        case 8: return launch<3, 8>(p, P, p->nitems, p->nsplits, s);
-        case 16: return launch<3, 16>(p, P, p->nitems, p->nsplits, s);
-        case 32: return launch<3, 32>(p, P, p->nitems, p->nsplits, s);
-        case 64: return launch<3, 64>(p, P, p->nitems, p->nsplits, s);
+        case 8: return launch<3, 8>(p, P, nlaunch, p->nsplits, s);
+        case 16: return launch<3, 16>(p, P, nlaunch, p->nsplits, s);
+        case 32: return launch<3, 32>(p, P, nlaunch, p->nsplits, s);
+        case 64: return launch<3, 64>(p, P, nlaunch, p->nsplits, s);
         }
     } else {
         switch (R) {
-        case 8: return launch<2, 8>(p, P, p->nitems, p->nsplits, s);
-        case 16: return launch<2, 16>(p, P, p->nitems, p->nsplits, s);
-        case 32: return launch<2, 32>(p, P, p->nitems, p->nsplits, s);
-        case 64: return launch<2, 64>(p, P, p->nitems, p->nsplits, s);
+        case 8: return launch<2, 8>(p, P, nlaunch, p->nsplits, s);
+        case 16: return launch<2, 16>(p, P, nlaunch, p->nsplits, s);
+        case 32: return launch<2, 32>(p, P, nlaunch, p->nsplits, s);
+        case 64: return launch<2, 64>(p, P, nlaunch, p->nsplits, s);
         }
     }
     return fail(FR_ERR_UNSUPPORTED, "coil group must be 4, 8, 16 or 32");

@@ -57,9 +57,11 @@ struct SplitTile {
     int pad;
 };
 
-// Scan tuple over tiles: pairs, work items, partial slots, split tiles.
+// Scan tuple over tiles: pairs, work items of occupied tiles, partial
+// slots, split tiles, empty tiles (whose zero-fill items follow every
+// occupied tile's items in the item list).
 struct TileScan {
-    long long pairs, items, slots, splits;
+    long long pairs, items, slots, splits, empties;
 };
 
 }  // namespace fr
@@ -82,6 +84,7 @@ struct fr_plan_s {
     size_t n = 0;
     bool planned = false;
     long long npairs = 0, nitems = 0, nslots = 0, nsplits = 0;
+    long long nitems_occupied = 0;  // items[0, nitems_occupied): tiles with samples; the rest zero-fill
     float bounds_host[12] = {0};  // raw lo[3], raw hi[3], norm lo[3], norm hi[3]
 
     fr::DevBuf lut_d;         // L floats

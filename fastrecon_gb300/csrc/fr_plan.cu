@@ -350,17 +350,19 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
 __device__ __forceinline__ TileScan tile_value(int cnt, int chunk)
 {
     TileScan v;
-    long long items = cnt == 0 ? 1 : (cnt + chunk - 1) / chunk;
+    long long items = (cnt + chunk - 1) / chunk;
     v.pairs = cnt;
     v.items = items;
     v.slots = items > 1 ? items : 0;
     v.splits = items > 1 ? 1 : 0;
+    v.empties = cnt == 0 ? 1 : 0;
     return v;
 }
 
 __device__ __forceinline__ TileScan add(const TileScan &a, const TileScan &b)
 {
-    return TileScan{a.pairs + b.pairs, a.items + b.items, a.slots + b.slots, a.splits + b.splits};
+    return TileScan{a.pairs + b.pairs, a.items + b.items, a.slots + b.slots, a.splits + b.splits,
+                    a.empties + b.empties};
 }
 
 __device__ __forceinline__ TileScan shfl_up(const TileScan &v, int d)
@@ -370,6 +372,7 @@ __device__ __forceinline__ TileScan shfl_up(const TileScan &v, int d)
     r.items = __shfl_up_sync(0xffffffffu, v.items, d);
     r.slots = __shfl_up_sync(0xffffffffu, v.slots, d);
     r.splits = __shfl_up_sync(0xffffffffu, v.splits, d);
+    r.empties = __shfl_up_sync(0xffffffffu, v.empties, d);
     return r;
 }
 
@@ -390,7 +393,7 @@ __device__ TileScan block_exclusive(TileScan v, TileScan *total)
     }
     if (lane == 31) warp_tot[warp] = inc;
     __syncthreads();
-    TileScan wpre{0, 0, 0, 0}, all{0, 0, 0, 0};
+    TileScan wpre{0, 0, 0, 0, 0}, all{0, 0, 0, 0, 0};
     for (int w = 0; w < kScanThreads / 32; ++w) {
         if (w < warp) wpre = add(wpre, warp_tot[w]);
         all = add(all, warp_tot[w]);
@@ -402,6 +405,7 @@ __device__ TileScan block_exclusive(TileScan v, TileScan *total)
     exc.items -= v.items;
     exc.slots -= v.slots;
     exc.splits -= v.splits;
+    exc.empties -= v.empties;
     return exc;
 }
 
@@ -423,11 +427,11 @@ __global__ void scan_reduce_kernel(const int *__restrict__ cnt, long long ntiles
 __global__ void scan_blocks_kernel(TileScan *sums, int nblocks)
 {
     __shared__ TileScan carry;
-    if (threadIdx.x == 0) carry = TileScan{0, 0, 0, 0};
+    if (threadIdx.x == 0) carry = TileScan{0, 0, 0, 0, 0};
     __syncthreads();
     for (int base = 0; base < nblocks; base += kScanThreads) {
         int i = base + threadIdx.x;
-        TileScan v = i < nblocks ? sums[i] : TileScan{0, 0, 0, 0};
+        TileScan v = i < nblocks ? sums[i] : TileScan{0, 0, 0, 0, 0};
         TileScan tot;
         TileScan exc = block_exclusive(v, &tot);
         TileScan c = carry;
@@ -448,7 +452,7 @@ __global__ void scan_write_kernel(const int *__restrict__ cnt, long long ntiles,
     TileScan v{0, 0, 0, 0};
     for (int k = 0; k < kScanPerThread; ++k) {
         long long t = t0 + k;
-        local[k] = t < ntiles ? tile_value(cnt[t], chunk) : TileScan{0, 0, 0, 0};
+        local[k] = t < ntiles ? tile_value(cnt[t], chunk) : TileScan{0, 0, 0, 0, 0};
         v = add(v, local[k]);
     }
     TileScan tot;
@@ -465,11 +469,21 @@ __global__ void items_kernel(const int *__restrict__ cnt, const TileScan *__rest
                              long long ntiles, int chunk, WorkItem *__restrict__ items,
                              SplitTile *__restrict__ splits)
 {
+    const long long occupied = scan[ntiles].items;  // the zero-fill items of empty tiles follow
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntiles;
          t += (long long)gridDim.x * blockDim.x) {
         int c = cnt[t];
         TileScan v = tile_value(c, chunk);
         TileScan o = scan[t];
+        if (c == 0) {
+            WorkItem w;
+            w.begin = o.pairs;
+            w.count = 0;
+            w.tile = (int)t;
+            w.slot = -1;
+            w.pad = 0;
+            items[occupied + o.empties] = w;
+        }
         for (long long k = 0; k < v.items; ++k) {
             WorkItem w;
             w.begin = o.pairs + k * chunk;
@@ -603,14 +617,15 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     for (int i = 0; i < 6; ++i) p->bounds_host[i] = raw_b[i];
     for (int i = 0; i < 6; ++i) p->bounds_host[6 + i] = prenorm ? raw_b[i] : norm_b[i];
 
-    if (tot.pairs > 0xFFFFFFFFll || tot.items > INT_MAX || tot.slots > INT_MAX)
+    if (tot.pairs > 0xFFFFFFFFll || tot.items + tot.empties > INT_MAX || tot.slots > INT_MAX)
         return fail(FR_ERR_UNSUPPORTED, "bin lists exceed 32-bit indexing");
     p->npairs = tot.pairs;
-    p->nitems = tot.items;
+    p->nitems = tot.items + tot.empties;
+    p->nitems_occupied = tot.items;
     p->nslots = tot.slots;
     p->nsplits = tot.splits;
     if (p->pairs.reserve(std::max<long long>(tot.pairs, 1) * 8) ||
-        p->items.reserve(std::max<long long>(tot.items, 1) * sizeof(WorkItem)) ||
+        p->items.reserve(std::max<long long>(p->nitems, 1) * sizeof(WorkItem)) ||
         p->splits.reserve(std::max<long long>(tot.splits, 1) * sizeof(SplitTile)))
         return FR_ERR_OUT_OF_MEMORY;
     if (n > 0) {
@@ -735,8 +750,9 @@ int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s,
     TileScan tot;
     FR_CUDA(cudaMemcpyAsync(&tot, pi.scan + pi.ntiles, sizeof(TileScan), cudaMemcpyDeviceToHost, s));
     FR_CUDA(cudaStreamSynchronize(s));
-    if (tot.pairs > 0xFFFFFFFFll || tot.items > INT_MAX || tot.slots > INT_MAX)
+    if (tot.pairs > 0xFFFFFFFFll || tot.items + tot.empties > INT_MAX || tot.slots > INT_MAX)
         return fail(FR_ERR_UNSUPPORTED, "bin lists exceed 32-bit indexing");
+    tot.items += tot.empties;  // every tile's items, the empty tiles' zero-fill items last
     // carve records, items and split tiles (256-byte aligned) from `rest`
     auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
     const size_t recs_b = align(std::max<long long>(tot.pairs, 1) * 8);
