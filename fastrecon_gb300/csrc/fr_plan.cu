@@ -177,6 +177,20 @@ __device__ __forceinline__ int sample_tiles(const BinGeom &g, const float4 &p, T
     return cnt ? w.n[0] * w.n[1] * w.n[2] : 0;
 }
 
+// Runs of consecutive lanes with the same tile (consecutive samples of a
+// readout usually share tiles): one counter update per run instead of one
+// per sample.  run: the run's length (valid in its first lane); head_lane:
+// the first lane of this lane's run.
+__device__ __forceinline__ void lane_runs(int t, int lane, int &run, int &head_lane)
+{
+    const int tp = __shfl_up_sync(0xffffffffu, t, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || tp != t);
+    const unsigned upto = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;  // lanes 0..lane
+    head_lane = 31 - __clz(heads & upto);
+    const unsigned after = heads & ~upto;
+    run = (after ? __ffs(after) - 1 : 32) - lane;
+}
+
 // Bin counters are striped: the samples of 32-sample group g count into
 // stripe g mod kStripes of a tile, so the many warps whose spokes all cross
 // the dense centre tiles spread their atomics over kStripes counters.  A
@@ -268,9 +282,9 @@ __global__ void normalize_count_kernel(const float4 *__restrict__ raw, size_t n,
         for (int j = 0; j < maxcnt; ++j, w.next()) {
             bool valid = j < cnt;
             int t = valid ? w.tile(g) : -1 - lane;
-            unsigned m = __match_any_sync(0xffffffffu, t);
-            int leader = __ffs(m) - 1;
-            if (valid && lane == leader) atomicAdd(&stripe_count[t * kStripes + stripe], __popc(m));
+            int run, head_lane;
+            lane_runs(t, lane, run, head_lane);
+            if (valid && lane == head_lane) atomicAdd(&stripe_count[t * kStripes + stripe], run);
         }
     }
 }
@@ -309,7 +323,6 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
                             unsigned long long *__restrict__ recs)
 {
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     for (size_t base = blockIdx.x * (size_t)blockDim.x; base < n;
          base += (size_t)gridDim.x * blockDim.x) {
         size_t i = base + threadIdx.x;
@@ -332,14 +345,14 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
         for (int j = 0; j < maxcnt; ++j, w.next()) {
             bool valid = j < cnt;
             int t = valid ? w.tile(g) : -1 - lane;
-            unsigned m = __match_any_sync(0xffffffffu, t);
-            int leader = __ffs(m) - 1;
+            int run, head_lane;
+            lane_runs(t, lane, run, head_lane);
             int basepos = 0;
             const int ts = t * kStripes + stripe;
-            if (valid && lane == leader) basepos = atomicAdd(&tile_fill[ts], __popc(m));
-            basepos = __shfl_sync(0xffffffffu, basepos, leader);
+            if (valid && lane == head_lane) basepos = atomicAdd(&tile_fill[ts], run);
+            basepos = __shfl_sync(0xffffffffu, basepos, head_lane);
             if (valid) {
-                long long pos = stripe_base[ts] + basepos + __popc(m & lt);
+                long long pos = stripe_base[ts] + basepos + (lane - head_lane);
                 unsigned box = tile_box(g, c, s, e, w.lo[0] + w.jx, w.lo[1] + w.jy, w.lo[2] + w.jz);
                 recs[pos] = ((unsigned long long)box << 32) | (unsigned long long)i;
             }
