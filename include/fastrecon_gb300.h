@@ -297,6 +297,7 @@ int fr_mlp_backward(const void *d_params_bf16, const float *d_features, const fl
  * BF16 copy. */
 int fr_mlp_adam(float *d_master, void *d_params_bf16, const float *d_grad, float *d_m, float *d_v, int count,
                 float lr, float beta1, float beta2, float eps, int step, void *stream);
+/* The BF16 copy of FP32 master parameters (round to nearest even). */
 int fr_mlp_to_bf16(const float *d_master, void *d_params_bf16, int count, void *stream);
 
 /* ------------------------------------------------------------------------
@@ -406,7 +407,8 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
 /* Plan object and grid workspace used by the recon (for stage timing). */
 int fr_recon_plan(fr_recon r, fr_plan *out_plan);
 /* Stage timings of the last fr_recon_run* call in ms (plan, grid, fft, sos),
- * measured with CUDA events when FR_TIMING=1 in the environment, else -1. */
+ * measured with CUDA events when FR_TIMING=1 in the environment, else -1.
+ * No counterpart in the reference, which prints its stages' wall times. */
 int fr_recon_stage_ms(fr_recon r, float *plan_ms, float *grid_ms, float *fft_ms, float *sos_ms);
 
 #ifdef __cplusplus
