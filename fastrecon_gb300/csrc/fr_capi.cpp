@@ -272,7 +272,8 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         delete p;
         return fail(FR_ERR_UNSUPPORTED, "too many tiles");
     }
-    p->chunk = d->chunk > 0 ? d->chunk : 4096;
+    p->chunk_req = d->chunk > 0 ? d->chunk : 0;
+    p->chunk = p->chunk_req > 0 ? p->chunk_req : 4096;
     {
         const char *cm = std::getenv("FR_KSPACE_COIL_MAJOR");
         p->kspace_sample_major = !(cm && std::atoi(cm) != 0);

@@ -77,7 +77,8 @@ struct fr_plan_s {
     int ntile[3] = {1, 1, 1};
     long long ntiles = 0;
     int coil_group = 8;
-    int chunk = 4096;
+    int chunk = 4096;       // records per work item of the current trajectory
+    int chunk_req = 0;      // the descriptor's chunk (0: chosen per trajectory, plan_chunk)
     int prefilter = 0;  // |x - c| >= kHW implies dk >= kHW (kHW^2 and sqrt exact)
     unsigned flags = 0;
 
@@ -188,6 +189,10 @@ struct PlanIntoOut {
     size_t rest_used;
 };
 long long plan_scan_blocks(long long ntiles);
+// Records per work item for n samples: enough items for every SM to take
+// several (a small trajectory's dense centre tile would otherwise be one
+// long item that the whole launch waits for), at most 4096.
+int plan_chunk(size_t n, int dim);
 int plan_stripes();  // bin-counter stripes per tile
 int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s, PlanIntoOut *out);
 

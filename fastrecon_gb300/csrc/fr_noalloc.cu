@@ -138,7 +138,7 @@ extern "C" int fr_grid_noalloc(const float *d_traj, size_t n, int dim, unsigned 
         pi.ntile[d] = ntile[d];
     }
     pi.ntiles = ntiles;
-    pi.chunk = 4096;
+    pi.chunk = plan_chunk(n, dim);
     pi.bounds = reinterpret_cast<int *>(scratch + off_bounds);
     pi.traj = reinterpret_cast<float4 *>(scratch + off_traj);
     pi.tile_count = reinterpret_cast<int *>(scratch + off_count);

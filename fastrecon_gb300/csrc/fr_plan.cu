@@ -562,6 +562,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
     if (n > 0xFFFFFFFFull) return fail(FR_ERR_UNSUPPORTED, "more than 2^32-1 samples");
     p->planned = false;
     p->n = n;
+    p->chunk = p->chunk_req > 0 ? p->chunk_req : plan_chunk(n, p->dim);
     if (p->bounds.reserve(kBoundsSlots * 4)) return FR_ERR_OUT_OF_MEMORY;
     if (p->traj.reserve(std::max<size_t>(n, 1) * 16)) return FR_ERR_OUT_OF_MEMORY;
     if (p->tile_count.reserve(p->ntiles * 4) || p->tile_fill.reserve(p->ntiles * kStripes * 4) ||
@@ -712,6 +713,20 @@ int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_o
 }
 
 int plan_stripes() { return kStripes; }
+
+int plan_chunk(size_t n, int dim)
+{
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 152;
+    // ~2.7 records per sample with 8^3 tiles in 3D, ~1.2 with 32^2 tiles in 2D;
+    // 2 CTAs per SM, at least 8 items each
+    const double records = (double)n * (dim == 3 ? 2.7 : 1.2);
+    const double per = records / ((double)sms * 2 * 8);
+    int c = 512;
+    while (c < 4096 && 2.0 * c <= per) c <<= 1;
+    return c;
+}
 
 long long plan_scan_blocks(long long ntiles)
 {
