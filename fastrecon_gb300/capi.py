@@ -106,6 +106,8 @@ _SIGS = {
     "fr_recon_destroy": (C.c_int, [_VP]),
     "fr_recon_run": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP]),
     "fr_recon_run_host": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP]),
+    "fr_recon_submit_host": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP]),
+    "fr_recon_sync": (C.c_int, [_VP, _VP]),
     "fr_recon_plan": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fr_recon_stage_ms": (C.c_int, [_VP, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                     C.POINTER(C.c_float)]),

@@ -38,8 +38,28 @@ struct fr_recon_s {
     // trajectory is planned
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_start = nullptr, copy_done = nullptr;
+    // submitted host-buffer volumes (fr_recon_submit_host): two staging
+    // slots, so volume i + 1 uploads while volume i is reconstructed and
+    // volume i - 1's image downloads
+    struct Slot {
+        DevBuf traj, dcf, kdata, img;
+        cudaEvent_t uploaded = nullptr;    // inputs on the device
+        cudaEvent_t consumed = nullptr;    // recon done with the inputs and wrote img
+        cudaEvent_t downloaded = nullptr;  // img copied to the host
+    } slot[2];
+    int next_slot = 0;
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
     ~fr_recon_s()
     {
+        if (up_stream) cudaStreamSynchronize(up_stream);
+        if (down_stream) cudaStreamSynchronize(down_stream);
+        for (auto &sl : slot) {
+            if (sl.consumed) cudaEventSynchronize(sl.consumed);
+            for (cudaEvent_t e : {sl.uploaded, sl.consumed, sl.downloaded})
+                if (e) cudaEventDestroy(e);
+        }
+        if (up_stream) cudaStreamDestroy(up_stream);
+        if (down_stream) cudaStreamDestroy(down_stream);
         if (copy_start) cudaEventDestroy(copy_start);
         if (copy_done) cudaEventDestroy(copy_done);
         if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -264,6 +284,63 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
     if (st) return st;
     FR_CUDA(cudaMemcpyAsync(h_image, r->h_img.ptr, nout * 4, cudaMemcpyDeviceToHost, s));
     FR_CUDA(cudaStreamSynchronize(s));
+    return FR_OK;
+}
+
+int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata, size_t n,
+                         float *h_image, void *stream)
+{
+    if (!r || !h_image || (n && (!h_traj || !h_dcf || !h_kdata)))
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (n > r->d.max_samples) return fail(FR_ERR_CAPACITY, "n exceeds max_samples");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nout = (size_t)r->d.out_size[0] * r->d.out_size[1] * r->d.out_size[2];
+    const size_t cap = r->d.max_samples > 0 ? r->d.max_samples : 1;
+    if (!r->up_stream) {
+        FR_CUDA(cudaStreamCreateWithFlags(&r->up_stream, cudaStreamNonBlocking));
+        FR_CUDA(cudaStreamCreateWithFlags(&r->down_stream, cudaStreamNonBlocking));
+        for (auto &sl : r->slot)
+            for (cudaEvent_t *e : {&sl.uploaded, &sl.consumed, &sl.downloaded})
+                FR_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
+    auto &sl = r->slot[r->next_slot];
+    if (sl.traj.reserve(cap * 16) || sl.dcf.reserve(cap * 4) || sl.kdata.reserve(cap * 8 * (size_t)r->d.channels) ||
+        sl.img.reserve(nout * 4))
+        return FR_ERR_OUT_OF_MEMORY;
+    r->next_slot ^= 1;
+    // upload once this slot's previous volume has been reconstructed (an
+    // event never recorded is complete)
+    FR_CUDA(cudaStreamWaitEvent(r->up_stream, sl.consumed, 0));
+    if (n) {
+        FR_CUDA(cudaMemcpyAsync(sl.traj.ptr, h_traj, n * 16, cudaMemcpyHostToDevice, r->up_stream));
+        FR_CUDA(cudaMemcpyAsync(sl.dcf.ptr, h_dcf, n * 4, cudaMemcpyHostToDevice, r->up_stream));
+        FR_CUDA(cudaMemcpyAsync(sl.kdata.ptr, h_kdata, n * 8 * (size_t)r->d.channels, cudaMemcpyHostToDevice,
+                                r->up_stream));
+    }
+    FR_CUDA(cudaEventRecord(sl.uploaded, r->up_stream));
+    // reconstruct once the inputs are there and the slot's previous image
+    // has left for the host
+    FR_CUDA(cudaStreamWaitEvent(s, sl.uploaded, 0));
+    FR_CUDA(cudaStreamWaitEvent(s, sl.downloaded, 0));
+    int st = recon_run(r, sl.traj.as<float>(), sl.dcf.as<float>(), sl.kdata.as<float>(), n, sl.img.as<float>(), s,
+                       nullptr);
+    if (st) {
+        fr_recon_sync(r, stream);  // leave nothing in flight on an error
+        return st;
+    }
+    FR_CUDA(cudaEventRecord(sl.consumed, s));
+    FR_CUDA(cudaStreamWaitEvent(r->down_stream, sl.consumed, 0));
+    FR_CUDA(cudaMemcpyAsync(h_image, sl.img.ptr, nout * 4, cudaMemcpyDeviceToHost, r->down_stream));
+    FR_CUDA(cudaEventRecord(sl.downloaded, r->down_stream));
+    return FR_OK;
+}
+
+int fr_recon_sync(fr_recon r, void *stream)
+{
+    if (!r) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    FR_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    if (r->up_stream) FR_CUDA(cudaStreamSynchronize(r->up_stream));
+    if (r->down_stream) FR_CUDA(cudaStreamSynchronize(r->down_stream));
     return FR_OK;
 }
 

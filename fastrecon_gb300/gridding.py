@@ -364,6 +364,20 @@ class Recon:
                                          C.c_void_p(_stream(stream))), "fr_recon_run_host")
         return out
 
+    def submit_host(self, traj, dcf, kdata, out, stream=None):
+        """Queues one volume of host (pinned) tensors and returns at once:
+        its upload and the previous image's download overlap the recon of
+        the volume before.  The tensors must stay alive and unchanged until
+        sync()."""
+        n = traj.shape[0]
+        check(self.lib.fr_recon_submit_host(self.h, _ptr(traj), _ptr(dcf), _ptr(kdata), n, _ptr(out),
+                                            C.c_void_p(_stream(stream))), "fr_recon_submit_host")
+        return out
+
+    def sync(self, stream=None):
+        """Waits until every submitted volume's image is in its host tensor."""
+        check(self.lib.fr_recon_sync(self.h, C.c_void_p(_stream(stream))), "fr_recon_sync")
+
     def _plan(self):
         h = C.c_void_p()
         check(self.lib.fr_recon_plan(self.h, C.byref(h)), "fr_recon_plan")

@@ -404,6 +404,18 @@ int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const floa
  * which returns once the image is in h_image. */
 int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata,
                       size_t n, float *h_image, void *stream);
+/* Pipelined form of fr_recon_run_host for a sequence of volumes (no
+ * counterpart in the reference, whose program reconstructs one data set per
+ * run): queues the upload of the inputs, the recon on `stream` and the
+ * download of the image, and returns without waiting.  Two device staging
+ * slots alternate, so the upload of one volume and the download of the
+ * previous image overlap the recon of the one in between.  The host buffers
+ * (pinned for overlap) must stay valid and unchanged until fr_recon_sync
+ * returns; the images equal fr_recon_run_host's bit for bit. */
+int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata,
+                         size_t n, float *h_image, void *stream);
+/* Waits until every submitted volume's image is in its host buffer. */
+int fr_recon_sync(fr_recon r, void *stream);
 /* Plan object and grid workspace used by the recon (for stage timing). */
 int fr_recon_plan(fr_recon r, fr_plan *out_plan);
 /* Stage timings of the last fr_recon_run* call in ms (plan, grid, fft, sos),
