@@ -411,7 +411,7 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
  * slots alternate, so the upload of one volume and the download of the
  * previous image overlap the recon of the one in between.  The host buffers
  * (pinned for overlap) must stay valid and unchanged until fr_recon_sync
- * returns; the images equal fr_recon_run_host's bit for bit. */
+ * returns; the images are fr_recon_run_host's. */
 int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata,
                          size_t n, float *h_image, void *stream);
 /* Waits until every submitted volume's image is in its host buffer. */
