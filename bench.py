@@ -328,7 +328,7 @@ def run_ours(args, w):
         for _ in range(2):
             rec.run_host(h_traj, h_dcf, h_kd, h_img)
         barrier()
-        k2 = max(3, min(args.steps, 20))
+        k2 = max(3, min(args.steps, 40))
         t0 = time.perf_counter()
         e0.record(stream)
         for _ in range(k2):
