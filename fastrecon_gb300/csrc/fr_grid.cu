@@ -730,30 +730,6 @@ void default_tiling(int dim, int *tile, int *coil_group, int channels)
     }
 }
 
-static bool kspace_transposable(fr_plan p, int channels)
-{
-    const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
-    return p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024;
-}
-
-int grid_prepare_kspace(fr_plan p, const float *d_kdata, int channels, cudaStream_t s)
-{
-    p->kt_src = nullptr;
-    if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "fr_grid called before fr_plan_set_trajectory");
-    if (!kspace_transposable(p, channels)) return FR_OK;
-    const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
-    if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2))) return FR_ERR_OUT_OF_MEMORY;
-    if (trsmem > 48 * 1024)
-        FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)trsmem));
-    transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
-        reinterpret_cast<const float2 *>(d_kdata), p->kt.as<float2>(), (long long)p->n, channels);
-    FR_CHECK_LAUNCH("transpose_kspace_kernel");
-    p->kt_src = d_kdata;
-    p->kt_channels = channels;
-    return FR_OK;
-}
-
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
              cudaStream_t s, bool skip_empty)
 {
@@ -793,12 +769,15 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.nwork = 0;
     P.sample_major = 0;
     P.skip_empty = skip_empty ? 1 : 0;
-    if (kspace_transposable(p, channels)) {
-        if (p->kt_src != d_kdata || p->kt_channels != channels) {
-            const int st = grid_prepare_kspace(p, d_kdata, channels, s);
-            if (st) return st;
-        }
-        p->kt_src = nullptr;  // one use
+    const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
+    if (p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024) {
+        if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2))) return FR_ERR_OUT_OF_MEMORY;
+        if (trsmem > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)trsmem));
+        transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
+            reinterpret_cast<const float2 *>(d_kdata), p->kt.as<float2>(), (long long)p->n, channels);
+        FR_CHECK_LAUNCH("transpose_kspace_kernel");
         P.kdata = p->kt.as<float>();
         P.sample_major = 1;
     }

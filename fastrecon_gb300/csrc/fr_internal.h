@@ -111,10 +111,6 @@ struct fr_plan_s {
     fr::DevBuf density_sat;   // G^d ints: per-cell counts -> summed-area table
     fr::DevBuf small;         // 256 bytes of scratch (feature max |k|)
     fr::DevBuf kt;            // n x channels complex: sample-major copy of the k-space (fr_grid)
-    // kt already holds the copy of this k-space (grid_prepare_kspace; the
-    // next grid_run of the same buffer and channels uses it once)
-    const float *kt_src = nullptr;
-    int kt_channels = 0;
     fr::DevBuf tile_mask;     // ntiles bits: tile holds bin records (recon path skips the others)
     bool kspace_sample_major = true;  // cleared by FR_KSPACE_COIL_MAJOR=1
 
@@ -132,10 +128,6 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
 // caller's next reader masks them with the plan's tile bitmap).
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
              cudaStream_t s, bool skip_empty = false);
-// The scatter's sample-major k-space copy made ahead of grid_run (on another
-// stream, e.g. while the previous volume is transformed); the caller orders
-// it before grid_run of the same d_kdata and channels.
-int grid_prepare_kspace(fr_plan p, const float *d_kdata, int channels, cudaStream_t s);
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
 // sos_mode: 2 = the whole SoS (sqrt, / deapod); for coils in slabs 0 = store
 // the plain sum of |x|^2, | 1 = add to the sum already in d_out.

@@ -561,7 +561,6 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         return fail(FR_ERR_INVALID_ARGUMENT, "trajectory pointer must be 16-byte aligned");
     if (n > 0xFFFFFFFFull) return fail(FR_ERR_UNSUPPORTED, "more than 2^32-1 samples");
     p->planned = false;
-    p->kt_src = nullptr;
     p->n = n;
     p->chunk = p->chunk_req > 0 ? p->chunk_req : plan_chunk(n, p->dim);
     if (p->bounds.reserve(kBoundsSlots * 4)) return FR_ERR_OUT_OF_MEMORY;

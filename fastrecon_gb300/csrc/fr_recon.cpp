@@ -24,7 +24,6 @@ struct fr_recon_s {
     bool checkerboard = false;
     std::vector<float> lut;
     fr_plan plan = nullptr;
-    fr_plan_desc plan_desc = {};  // for the pipeline slots' own plans
     fr_fft fft = nullptr;
     fr_fft fft1 = nullptr;  // single-image plan for the deapodization map
     fr_fftcs pruned = nullptr;  // pruned FFT + crop + SoS (even G)
@@ -44,9 +43,8 @@ struct fr_recon_s {
     // volume i - 1's image downloads
     struct Slot {
         DevBuf traj, dcf, kdata, img;
-        fr_plan plan = nullptr;            // this slot's binning (planned on the upload stream)
-        cudaEvent_t uploaded = nullptr;    // inputs on the device, planned, k-space copy made
-        cudaEvent_t consumed = nullptr;    // recon done with the inputs and the plan, wrote img
+        cudaEvent_t uploaded = nullptr;    // inputs on the device
+        cudaEvent_t consumed = nullptr;    // recon done with the inputs and wrote img
         cudaEvent_t downloaded = nullptr;  // img copied to the host
     } slot[2];
     int next_slot = 0;
@@ -59,7 +57,6 @@ struct fr_recon_s {
             if (sl.consumed) cudaEventSynchronize(sl.consumed);
             for (cudaEvent_t e : {sl.uploaded, sl.consumed, sl.downloaded})
                 if (e) cudaEventDestroy(e);
-            if (sl.plan) fr_plan_destroy(sl.plan);
         }
         if (up_stream) cudaStreamDestroy(up_stream);
         if (down_stream) cudaStreamDestroy(down_stream);
@@ -117,7 +114,6 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
     }
     pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
     st = fr_plan_create(&pd, &r->plan);
-    r->plan_desc = pd;  // pd.lut points into r->lut, which lives as long as r
     // the pruned transform with fused crop + SoS where it is specialised for
     // G (faster than cuFFT + SoS there), or when asked for
     const bool want_pruned = (d->flags & FR_RECON_PRUNED_FFT) || pruned_fft_specialised((int)r->G);
@@ -173,13 +169,10 @@ static int ensure_deapod(fr_recon r, cudaStream_t s)
 }  // extern "C"
 
 namespace {
-// The recon of fr_recon_run with plan `p`; `kdata_ready` (if given) is
-// waited for on the stream between planning and gridding.  `planned`: p
-// already holds this trajectory's binning (and, where the scatter uses one,
-// the sample-major k-space copy), made on another stream that the caller has
-// ordered before `s`.
-int recon_run(fr_recon r, fr_plan p, bool planned, const float *d_traj, const float *d_dcf, const float *d_kdata,
-              size_t n, float *d_image, cudaStream_t s, cudaEvent_t kdata_ready)
+// The recon of fr_recon_run; `kdata_ready` (if given) is waited for on the
+// stream between planning and gridding.
+int recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *d_kdata, size_t n, float *d_image,
+              cudaStream_t s, cudaEvent_t kdata_ready)
 {
     void *stream = (void *)s;
     int st = FR_OK;
@@ -190,7 +183,7 @@ int recon_run(fr_recon r, fr_plan p, bool planned, const float *d_traj, const fl
     unsigned sz[3] = {r->G, r->G, r->d.dim == 3 ? r->G : 1u};
     float *g = r->grid.as<float>();
     if (r->timing) cudaEventRecord(r->ev[0], s);
-    if (!planned) st = fr_plan_set_trajectory(p, d_traj, n, stream);
+    st = fr_plan_set_trajectory(r->plan, d_traj, n, stream);
     if (r->timing) cudaEventRecord(r->ev[1], s);
     if (!st && kdata_ready) {
         cudaError_t e = cudaStreamWaitEvent(s, kdata_ready, 0);
@@ -206,6 +199,7 @@ int recon_run(fr_recon r, fr_plan p, bool planned, const float *d_traj, const fl
     // so the scatter leaves tiles without samples unwritten (for the
     // kooshball about half the 384^3 grid: its corners).
     TileMask tm;
+    const fr_plan p = r->plan;
     const bool pow2 = ((p->tile[0] | p->tile[1] | p->tile[2]) > 0) && !(p->tile[0] & (p->tile[0] - 1)) &&
                       !(p->tile[1] & (p->tile[1] - 1)) && !(p->tile[2] & (p->tile[2] - 1));
     const bool skip = r->pruned && fftcs_masks_tiles(r->pruned) && pow2;
@@ -220,7 +214,7 @@ int recon_run(fr_recon r, fr_plan p, bool planned, const float *d_traj, const fl
     for (int c0 = 0; !st && c0 < C; c0 += r->slab) {
         const int cs = std::min(r->slab, C - c0);
         const int mode = (c0 > 0 ? 1 : 0) | (c0 + cs == C ? 2 : 0);
-        st = grid_run(p, d_kdata + 2 * (size_t)c0 * n, d_dcf, cs, g, s, skip);
+        st = grid_run(r->plan, d_kdata + 2 * (size_t)c0 * n, d_dcf, cs, g, s, skip);
         if (r->timing && c0 == 0) cudaEventRecord(r->ev[2], s);
         if (r->pruned) {
             // transform, crop and SoS in one pruned pass (the stage times are
@@ -251,7 +245,7 @@ int fr_recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const floa
 {
     if (!r || !d_image || (n && (!d_traj || !d_dcf || !d_kdata)))
         return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
-    return recon_run(r, r->plan, false, d_traj, d_dcf, d_kdata, n, d_image, (cudaStream_t)stream, nullptr);
+    return recon_run(r, d_traj, d_dcf, d_kdata, n, d_image, (cudaStream_t)stream, nullptr);
 }
 
 int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata, size_t n,
@@ -284,7 +278,7 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
         FR_CUDA(cudaMemcpyAsync(r->h_traj.ptr, h_traj, n * 16, cudaMemcpyHostToDevice, s));
         FR_CUDA(cudaMemcpyAsync(r->h_dcf.ptr, h_dcf, n * 4, cudaMemcpyHostToDevice, s));
     }
-    int st = recon_run(r, r->plan, false, r->h_traj.as<float>(), r->h_dcf.as<float>(), r->h_kdata.as<float>(), n,
+    int st = recon_run(r, r->h_traj.as<float>(), r->h_dcf.as<float>(), r->h_kdata.as<float>(), n,
                        r->h_img.as<float>(), s, ready);
     if (st && ready) cudaStreamSynchronize(r->copy_stream);  // leave no copy in flight on an error
     if (st) return st;
@@ -313,16 +307,9 @@ int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, co
     if (sl.traj.reserve(cap * 16) || sl.dcf.reserve(cap * 4) || sl.kdata.reserve(cap * 8 * (size_t)r->d.channels) ||
         sl.img.reserve(nout * 4))
         return FR_ERR_OUT_OF_MEMORY;
-    if (!sl.plan) {
-        int st = fr_plan_create(&r->plan_desc, &sl.plan);
-        if (st) return st;
-        sl.plan->kspace_sample_major = r->plan->kspace_sample_major;
-    }
     r->next_slot ^= 1;
     // upload once this slot's previous volume has been reconstructed (an
-    // event never recorded is complete), then plan the trajectory and make
-    // the scatter's k-space copy on the upload stream too: all of it
-    // overlaps the previous volume's scatter and transform on `s`
+    // event never recorded is complete)
     FR_CUDA(cudaStreamWaitEvent(r->up_stream, sl.consumed, 0));
     if (n) {
         FR_CUDA(cudaMemcpyAsync(sl.traj.ptr, h_traj, n * 16, cudaMemcpyHostToDevice, r->up_stream));
@@ -330,19 +317,13 @@ int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, co
         FR_CUDA(cudaMemcpyAsync(sl.kdata.ptr, h_kdata, n * 8 * (size_t)r->d.channels, cudaMemcpyHostToDevice,
                                 r->up_stream));
     }
-    int st = fr_plan_set_trajectory(sl.plan, sl.traj.as<float>(), n, r->up_stream);
-    if (!st && r->slab == r->d.channels) st = grid_prepare_kspace(sl.plan, sl.kdata.as<float>(), r->d.channels, r->up_stream);
-    if (st) {
-        fr_recon_sync(r, stream);
-        return st;
-    }
     FR_CUDA(cudaEventRecord(sl.uploaded, r->up_stream));
     // reconstruct once the inputs are there and the slot's previous image
     // has left for the host
     FR_CUDA(cudaStreamWaitEvent(s, sl.uploaded, 0));
     FR_CUDA(cudaStreamWaitEvent(s, sl.downloaded, 0));
-    st = recon_run(r, sl.plan, true, sl.traj.as<float>(), sl.dcf.as<float>(), sl.kdata.as<float>(), n,
-                   sl.img.as<float>(), s, nullptr);
+    int st = recon_run(r, sl.traj.as<float>(), sl.dcf.as<float>(), sl.kdata.as<float>(), n, sl.img.as<float>(), s,
+                       nullptr);
     if (st) {
         fr_recon_sync(r, stream);  // leave nothing in flight on an error
         return st;

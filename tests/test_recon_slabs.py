@@ -87,9 +87,8 @@ def test_register_fft_masks_unwritten_tiles():
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", [dict(), dict(use_cufft=True)])
 def test_submitted_volumes_with_slabs(mode):
-    """fr_recon_submit_host with coils in slabs (the scatter's k-space copy is
-    then made per slab on the recon stream instead of ahead on the upload
-    stream): equal to one fr_recon_run_host per volume."""
+    """fr_recon_submit_host with coils in slabs: equal to one
+    fr_recon_run_host per volume."""
     import torch
     c = load_case("koosh3d_small")
     if c["coils"] < 2:
