@@ -56,6 +56,10 @@ struct GridParams {
     // a record's coil values are one contiguous run instead of one value per
     // coil plane
     int sample_major;
+    // k-space values already multiplied by the DCF (the sample-major copy),
+    // with mag[s] = max over the sample's coil floats of |dcf * k|: the
+    // per-item scale then needs one float per record
+    const float *mag;
     int skip_empty;     // tiles without samples are left unwritten
 };
 
@@ -328,6 +332,32 @@ __device__ __forceinline__ void scale_bounds(const unsigned long long *recs, int
     }
 }
 
+// The bound of scale_bounds from the per-sample magnitudes mag[s] >= every
+// |dcf * k_f| of sample s, one record per lane: one B and M for all coil
+// floats of the item.  Also pulls each record's position into L1.
+template <int NW>
+__device__ __forceinline__ void scale_bounds_mag(const unsigned long long *recs, int count, int warp, int lane,
+                                                 const float4 *traj, const float *mag, float &bs, float &bm)
+{
+    bs = bm = 0.f;
+    for (int j = warp * 32 + lane; j < count; j += NW * 32) {
+        const unsigned long long rec = recs[j];
+        const unsigned box = (unsigned)(rec >> 32);
+        const unsigned sl = (unsigned)rec;
+        if (((box >> 18) & 15) * ((box >> 22) & 15) * ((box >> 26) & 15) != 0) {
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(traj + sl));
+            const float a = mag[sl];
+            bs += a;
+            bm = fmaxf(bm, a);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bs += __shfl_xor_sync(0xffffffffu, bs, o);
+        bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+    }
+}
+
 // 1 / S_f from the item's B_f and M_f (exact: a power of two).
 __device__ __forceinline__ float inv_scale_of(float bsum, unsigned bmax_bits, float lut_absmax)
 {
@@ -419,7 +449,17 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     const size_t ks = P.sample_major ? 2 * (size_t)P.channels : 2;
     const unsigned long long *recs = P.recs + it.begin;
 
-    {
+    if (P.mag) {
+        float bs, bm;
+        scale_bounds_mag<kWarps>(recs, it.count, warp, lane, traj, P.mag + s_off, bs, bm);
+        if (lane == 0) {
+            atomicAdd(&bsum_s[0], bs);
+            atomicMax(&bmax_s[0], __float_as_uint(bm));
+        }
+        __syncthreads();
+        if (threadIdx.x < R) inv_s[threadIdx.x] = inv_scale_of(bsum_s[0], bmax_s[0], P.lut_absmax);
+        __syncthreads();
+    } else {
         float bs[NF], bm[NF];
         scale_bounds<NF, kWarps, true>(recs, it.count, warp, lane, traj, dcf, kdf, ks, coil_ok, bs, bm);
         if (q == 0) {
@@ -435,6 +475,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         if (threadIdx.x < R) inv_s[threadIdx.x] = inv_scale_of(bsum_s[threadIdx.x], bmax_s[threadIdx.x], P.lut_absmax);
         __syncthreads();
     }
+    const bool premul = P.mag != nullptr;
     float sc[NF];
 #pragma unroll
     for (int k = 0; k < NF; ++k) sc[k] = __fdiv_rn(1.f, inv_s[f0 + 32 * k]);  // exact
@@ -450,11 +491,14 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
         const int ntap = nx * ny * nz;
         if (ntap == 0) continue;
         const float4 p = traj[s];
-        const float d = dcf[s];
+        // GridLut.cpp:109 dcf * k (made by the k-space copy when premultiplied: the same product), scaled
+        const float d = premul ? 1.f : dcf[s];
         float val[NF];
 #pragma unroll
-        for (int k = 0; k < NF; ++k)
-            val[k] = coil_ok[k] ? __fmul_rn(__fmul_rn(d, kdf[k][ks * s]), sc[k]) : 0.f;  // GridLut.cpp:109, scaled
+        for (int k = 0; k < NF; ++k) {
+            const float dk = premul ? kdf[k][ks * s] : __fmul_rn(d, kdf[k][ks * s]);
+            val[k] = coil_ok[k] ? __fmul_rn(dk, sc[k]) : 0.f;
+        }
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
         const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 4);
         // box origin as floats (integers below 2^24: exact), its first cell
@@ -638,13 +682,19 @@ __global__ void reduce_splits_kernel(GridParams P)
 // bound by the latency of these reads).
 constexpr int kTrSamples = 128;
 constexpr int kTrThreads = 256, kTrPer = 8;
+// The copy holds dcf * k (the product GridLut.cpp:109 forms, same rounding)
+// and mag[s] = the largest |re| or |im| of sample s's products.
 __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const float2 *__restrict__ in,
-                                                                      float2 *__restrict__ out, long long n,
+                                                                      const float *__restrict__ dcf,
+                                                                      float2 *__restrict__ out,
+                                                                      float *__restrict__ mag, long long n,
                                                                       int channels)
 {
     extern __shared__ float2 tr[];  // [channels][kTrSamples + 1]
+    __shared__ float dsh[kTrSamples];
     const long long s0 = (long long)blockIdx.x * kTrSamples;
     const int ns = (int)min((long long)kTrSamples, n - s0);
+    for (int j = threadIdx.x; j < ns; j += kTrThreads) dsh[j] = dcf[s0 + j];
     const int total = channels * kTrSamples;
     for (int i0 = 0; i0 < total; i0 += kTrThreads * kTrPer) {
         float2 v[kTrPer];
@@ -663,7 +713,18 @@ __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const floa
     __syncthreads();
     for (int i = threadIdx.x; i < channels * ns; i += kTrThreads) {
         const int j = i / channels, c = i - j * channels;
-        out[(size_t)(s0 + j) * channels + c] = tr[c * (kTrSamples + 1) + j];
+        const float2 v = tr[c * (kTrSamples + 1) + j];
+        const float d = dsh[j];
+        out[(size_t)(s0 + j) * channels + c] = make_float2(__fmul_rn(d, v.x), __fmul_rn(d, v.y));
+    }
+    for (int j = threadIdx.x; j < ns; j += kTrThreads) {
+        const float d = dsh[j];
+        float m = 0.f;
+        for (int c = 0; c < channels; ++c) {
+            const float2 v = tr[c * (kTrSamples + 1) + j];
+            m = fmaxf(m, fmaxf(fabsf(__fmul_rn(d, v.x)), fabsf(__fmul_rn(d, v.y))));
+        }
+        mag[s0 + j] = m;
     }
 }
 
@@ -770,16 +831,20 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.sample_major = 0;
     P.skip_empty = skip_empty ? 1 : 0;
     const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
+    P.mag = nullptr;
     if (p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024) {
-        if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2))) return FR_ERR_OUT_OF_MEMORY;
+        if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2)) || p->kmag.reserve(p->n * sizeof(float)))
+            return FR_ERR_OUT_OF_MEMORY;
         if (trsmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsmem));
         transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
-            reinterpret_cast<const float2 *>(d_kdata), p->kt.as<float2>(), (long long)p->n, channels);
+            reinterpret_cast<const float2 *>(d_kdata), d_dcf, p->kt.as<float2>(), p->kmag.as<float>(),
+            (long long)p->n, channels);
         FR_CHECK_LAUNCH("transpose_kspace_kernel");
         P.kdata = p->kt.as<float>();
         P.sample_major = 1;
+        P.mag = p->kmag.as<float>();
     }
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;
@@ -874,6 +939,7 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.work_counter = nullptr;
     P.nwork = 0;
     P.sample_major = 0;
+    P.mag = nullptr;
     P.skip_empty = 0;
     if (gi.nitems == 0) return FR_OK;
     if (gi.dim == 3) {
@@ -988,6 +1054,7 @@ int batch_grid_run(const BatchGrid &b, const float *d_kdata, const float *d_dcf,
     P.work_counter = b.work_counter;
     P.nwork = b.nitems * P.ngroups;
     P.sample_major = 0;
+    P.mag = nullptr;
     P.skip_empty = 0;
     if (P.nwork == 0) return FR_OK;
     if (P.nwork > 0x7FFFFFFFll) return fail(FR_ERR_UNSUPPORTED, "too many work items");

@@ -110,7 +110,8 @@ struct fr_plan_s {
     fr::DevBuf real_partials; // nslots * K floats: split tiles of the real-valued scatter
     fr::DevBuf density_sat;   // G^d ints: per-cell counts -> summed-area table
     fr::DevBuf small;         // 256 bytes of scratch (feature max |k|)
-    fr::DevBuf kt;            // n x channels complex: sample-major copy of the k-space (fr_grid)
+    fr::DevBuf kt;            // n x channels complex: sample-major copy of dcf * k-space (fr_grid)
+    fr::DevBuf kmag;          // n floats: per sample max |re|, |im| of dcf * k over the coils
     fr::DevBuf tile_mask;     // ntiles bits: tile holds bin records (recon path skips the others)
     bool kspace_sample_major = true;  // cleared by FR_KSPACE_COIL_MAJOR=1
 
