@@ -634,46 +634,105 @@ __global__ void __launch_bounds__(512) grid_persistent_kernel(GridParams P)
 }
 
 // Sum the partial tiles of each split tile in item order and write the grid.
+// CTA (split tile, coil group, part): part z of kReduceParts holds a run of
+// the tile's rows.  The partial rows are read as contiguous float4 ([cell][R]
+// swizzled, as the scatter wrote them), summed slot after slot (the float
+// order of a plain loop over the items), staged in shared memory, and written
+// as x pairs of one coil per thread, each pair's offset computed once.
+constexpr int kReduceParts = 4, kReduceThreads = 256;
+
 template <int R>
-__global__ void reduce_splits_kernel(GridParams P)
+__global__ void __launch_bounds__(kReduceThreads) reduce_splits_kernel(GridParams P)
 {
+    extern __shared__ float4 red_raw[];
+    float *sum = reinterpret_cast<float *>(red_raw);
     const SplitTile st = P.splits[blockIdx.x];
     const int cg = blockIdx.y;
     const int t = st.tile;
-    const int ox = (t % P.ntile[0]) * P.tile[0];
-    const int oy = ((t / P.ntile[0]) % P.ntile[1]) * P.tile[1];
-    const int oz = (t / (P.ntile[0] * P.ntile[1])) * P.tile[2];
+    const int Tx = P.tile[0], Ty = P.tile[1];
+    const int rows = Ty * P.tile[2];
+    const int nparts = gridDim.z;
+    const int r0 = rows * (int)blockIdx.z / nparts, r1 = rows * ((int)blockIdx.z + 1) / nparts;
+    const int c0 = r0 * Tx, ncell = (r1 - r0) * Tx;
     const int K = P.K, CG = P.coil_group;
-    const size_t G = (size_t)P.G;
-    const size_t cells = P.dim == 3 ? G * G * G : G * G;
-    float2 *grid = reinterpret_cast<float2 *>(P.grid + (P.frame_off ? (size_t)st.pad * (size_t)P.grid_frame_floats : 0));
-    const size_t slot_stride = (size_t)P.ngroups * K * R;
-    const float *base = P.partials + ((size_t)st.first_slot * P.ngroups + cg) * (size_t)K * R;
-    const int total = CG * K;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        int cl = idx / K;
-        int i = idx - cl * K;
-        int c = cg * CG + cl;
-        if (c >= P.channels) break;
-        int lx = i % P.tile[0];
-        int r = i / P.tile[0];
-        int ly = r % P.tile[1];
-        int lz = r / P.tile[1];
-        int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        if (gx >= P.G || gy >= P.G || gz >= (P.dim == 3 ? P.G : 1)) continue;
-        int col = (2 * cl) ^ swz<R>(i);
-        float2 v = make_float2(0.f, 0.f);
-        for (int k = 0; k < st.nslots; ++k) {
-            float2 a = *reinterpret_cast<const float2 *>(base + k * slot_stride + (size_t)i * R + col);
-            v.x = __fadd_rn(v.x, a.x);
-            v.y = __fadd_rn(v.y, a.y);
+    const int ox = (t % P.ntile[0]) * Tx;
+    const int oy = ((t / P.ntile[0]) % P.ntile[1]) * Ty;
+    const int oz = (t / (P.ntile[0] * P.ntile[1])) * P.tile[2];
+    const size_t stride4 = (size_t)P.ngroups * K * R / 4;
+    const float4 *src = reinterpret_cast<const float4 *>(P.partials) +
+                        ((size_t)st.first_slot * P.ngroups + cg) * (size_t)K * R / 4 + (size_t)c0 * R / 4;
+    const int n4 = ncell * R / 4;
+    for (int i = threadIdx.x; i < n4; i += kReduceThreads) {
+        float4 v = src[i];
+        int k = 1;
+        for (; k + 4 <= st.nslots; k += 4) {
+            const float4 a0 = src[(size_t)k * stride4 + i], a1 = src[(size_t)(k + 1) * stride4 + i];
+            const float4 a2 = src[(size_t)(k + 2) * stride4 + i], a3 = src[(size_t)(k + 3) * stride4 + i];
+            v = make_float4(__fadd_rn(v.x, a0.x), __fadd_rn(v.y, a0.y), __fadd_rn(v.z, a0.z), __fadd_rn(v.w, a0.w));
+            v = make_float4(__fadd_rn(v.x, a1.x), __fadd_rn(v.y, a1.y), __fadd_rn(v.z, a1.z), __fadd_rn(v.w, a1.w));
+            v = make_float4(__fadd_rn(v.x, a2.x), __fadd_rn(v.y, a2.y), __fadd_rn(v.z, a2.z), __fadd_rn(v.w, a2.w));
+            v = make_float4(__fadd_rn(v.x, a3.x), __fadd_rn(v.y, a3.y), __fadd_rn(v.z, a3.z), __fadd_rn(v.w, a3.w));
         }
+        for (; k < st.nslots; ++k) {
+            const float4 a = src[(size_t)k * stride4 + i];
+            v = make_float4(__fadd_rn(v.x, a.x), __fadd_rn(v.y, a.y), __fadd_rn(v.z, a.z), __fadd_rn(v.w, a.w));
+        }
+        red_raw[i] = v;
+    }
+    __syncthreads();
+    const size_t G = (size_t)P.G;
+    const int Gz = P.dim == 3 ? P.G : 1;
+    const size_t cells = P.dim == 3 ? G * G * G : G * G;
+    const int ncl = min(CG, P.channels - cg * CG);
+    float *gridf = P.grid + (P.frame_off ? (size_t)st.pad * (size_t)P.grid_frame_floats : 0);
+    const int npair = ncell / 2;
+    if ((Tx % 2) == 0 && (P.G % 2) == 0 && kReduceThreads % npair == 0 &&
+        (reinterpret_cast<uintptr_t>(gridf) & 15) == 0) {
+        const int slot = threadIdx.x % npair, cstep = kReduceThreads / npair;
+        const int lx = 2 * (slot % (Tx / 2)), r = r0 + slot / (Tx / 2);
+        const int gx = ox + lx, gy = oy + r % Ty, gz = oz + r / Ty;
+        if (gx >= P.G || gy >= P.G || gz >= Gz) return;  // gx even, G even: gx + 1 < G as well
+        float4 *gridc = reinterpret_cast<float4 *>(gridf) + ((((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1);
+        const int i = r * Tx + lx, il = i - c0;
+        const int swa = swz<R>(i), swb = swz<R>(i + 1);
+        const float sa = P.checkerboard && ((gx + gy + gz) & 1) ? -1.f : 1.f;
+        const float sb = P.checkerboard ? -sa : 1.f;
+        for (int cl = threadIdx.x / npair; cl < ncl; cl += cstep) {
+            const float2 a = *reinterpret_cast<const float2 *>(sum + il * R + ((2 * cl) ^ swa));
+            const float2 b = *reinterpret_cast<const float2 *>(sum + (il + 1) * R + ((2 * cl) ^ swb));
+            gridc[(size_t)(cg * CG + cl) * (cells >> 1)] = make_float4(a.x * sa, a.y * sa, b.x * sb, b.y * sb);
+        }
+        return;
+    }
+    float2 *grid = reinterpret_cast<float2 *>(gridf);
+    for (int idx = threadIdx.x; idx < ncl * ncell; idx += kReduceThreads) {
+        const int cl = idx / ncell, il = idx - cl * ncell, i = c0 + il;
+        const int lx = i % Tx, r = i / Tx;
+        const int gx = ox + lx, gy = oy + r % Ty, gz = oz + r / Ty;
+        if (gx >= P.G || gy >= P.G || gz >= Gz) continue;
+        float2 v = *reinterpret_cast<const float2 *>(sum + il * R + ((2 * cl) ^ swz<R>(i)));
         if (P.checkerboard && ((gx + gy + gz) & 1)) {
             v.x = -v.x;
             v.y = -v.y;
         }
-        grid[(size_t)c * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+        grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
     }
+}
+
+// The reduction of the split tiles (none: nothing to launch).
+template <int R>
+int launch_reduce(const GridParams &P, long long nsplits, cudaStream_t s)
+{
+    if (nsplits <= 0) return FR_OK;
+    const int rows = P.tile[1] * P.tile[2];
+    const int parts = rows % kReduceParts == 0 ? kReduceParts : 1;
+    const size_t smem = (size_t)(rows / parts) * P.tile[0] * R * sizeof(float);
+    if (smem > 48 * 1024)
+        FR_CUDA(cudaFuncSetAttribute(reduce_splits_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 g2((unsigned)nsplits, (unsigned)P.ngroups, (unsigned)parts);
+    reduce_splits_kernel<R><<<g2, kReduceThreads, smem, s>>>(P);
+    FR_CHECK_LAUNCH("reduce_splits_kernel");
+    return FR_OK;
 }
 
 // [channels][n] complex -> [n][channels] complex, kTrSamples samples per CTA
@@ -753,12 +812,7 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
     kern<<<grid, threads, smem, s>>>(P);
     FR_CHECK_LAUNCH("grid_tiles_kernel");
     if (ev) FR_CUDA(cudaEventRecord(ev[1], s));
-    if (nsplits > 0) {
-        dim3 g2((unsigned)nsplits, (unsigned)P.ngroups);
-        reduce_splits_kernel<R><<<g2, 256, 0, s>>>(P);
-        FR_CHECK_LAUNCH("reduce_splits_kernel");
-    }
-    return FR_OK;
+    return launch_reduce<R>(P, nsplits, s);
 }
 
 }  // namespace
@@ -887,12 +941,7 @@ int launch_into(const GridParams &P, long long nitems, long long nsplits, cudaSt
     dim3 grid((unsigned)nitems, (unsigned)P.ngroups);
     kern<<<grid, kWarps * 32, smem, s>>>(P);
     FR_CHECK_LAUNCH("grid_tiles_kernel");
-    if (nsplits > 0) {
-        dim3 g2((unsigned)nsplits, (unsigned)P.ngroups);
-        reduce_splits_kernel<R><<<g2, 256, 0, s>>>(P);
-        FR_CHECK_LAUNCH("reduce_splits_kernel");
-    }
-    return FR_OK;
+    return launch_reduce<R>(P, nsplits, s);
 }
 }  // namespace
 
@@ -987,12 +1036,7 @@ int batch_launch_t(const GridParams &P, int blocks, long long nsplits, cudaStrea
     const long long nb = std::min<long long>(blocks, P.nwork);
     grid_persistent_kernel<DIM, R><<<(unsigned)nb, kWarps * 32, smem, s>>>(P);
     FR_CHECK_LAUNCH("grid_persistent_kernel");
-    if (nsplits > 0) {
-        dim3 g2((unsigned)nsplits, (unsigned)P.ngroups);
-        reduce_splits_kernel<R><<<g2, 256, 0, s>>>(P);
-        FR_CHECK_LAUNCH("reduce_splits_kernel");
-    }
-    return FR_OK;
+    return launch_reduce<R>(P, nsplits, s);
 }
 }  // namespace
 
