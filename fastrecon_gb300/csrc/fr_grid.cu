@@ -249,25 +249,24 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
 constexpr int kWarps = 16;         // 512 threads per CTA
 constexpr int kListEntries = 32;   // per warp and buffer
 constexpr int kScaleBatch = 4;     // records per warp step of the scale pass
-constexpr int kDecBytes = 16 * 64 * 4;  // tap decode table: 16 box classes x 64 taps x 32-bit word
+constexpr int kDecBytes = 16 * 64 * 16;  // tap decode table: 16 box classes x 64 taps x float4
 
 // Shared-memory layout of the scatter: accumulator tile [K][R] int32 | LUT
 // entries [L] float4 | per warp two tap-list buffers [32] {shared address of
-// the tap's cell row (swizzled), weight} | tap decode table [16][64] words |
+// the tap's cell row (swizzled), weight} | tap decode table [16][64] float4 |
 // per coil float: bound sum, bound max, inverse scale [3][64] floats.
 //
 // Decode table: for a tap box of nx x ny x nz cells (nx, ny <= 4; class
-// (nx-1)*4 + (ny-1)), tap tt = ix + nx (iy + ny iz) is the word ix | iy << 4 |
-// iz << 8 | cell offset ((iz Ty + iy) Tx + ix) << 12: one 4-byte entry per
-// lane keeps the lookup at one shared-memory wavefront per warp.  Built
-// without divisions: t / n for n <= 4 and t < 64 is
-// (t * {128, 64, 43, 32}[n-1]) >> 7.
+// (nx-1)*4 + (ny-1)), tap tt = ix + nx (iy + ny iz) is the float4 {ix, iy,
+// iz, cell offset (iz Ty + iy) Tx + ix as int bits}: one 16-byte load per
+// lane, no unpacking or conversions.  Built without divisions: t / n for
+// n <= 4 and t < 64 is (t * {128, 64, 43, 32}[n-1]) >> 7.
 template <int R>
 __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
 {
     float4 *lutE_g = reinterpret_cast<float4 *>(reinterpret_cast<float *>(smem4) + (size_t)P.K * R);
-    unsigned *dec_g = reinterpret_cast<unsigned *>(reinterpret_cast<unsigned char *>(lutE_g + P.L) +
-                                                   kWarps * 2 * kListEntries * 8);
+    float4 *dec_g = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(lutE_g + P.L) +
+                                               kWarps * 2 * kListEntries * 8);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutE_g[i] = P.lut_e[i];
     const int Tx = P.tile[0], Ty = P.tile[1];
     for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
@@ -277,7 +276,7 @@ __device__ __forceinline__ void stage_tables(const GridParams &P, float4 *smem4)
         const int my = ny == 1 ? 128 : ny == 2 ? 64 : ny == 3 ? 43 : 32;
         const int q1 = (tt * mx) >> 7, ix = tt - q1 * nx;
         const int iz = (q1 * my) >> 7, iy = q1 - iz * ny;
-        dec_g[i] = (unsigned)ix | ((unsigned)iy << 4) | ((unsigned)iz << 8) | ((unsigned)((iz * Ty + iy) * Tx + ix) << 12);
+        dec_g[i] = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
     }
 }
 
@@ -500,7 +499,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             val[k] = coil_ok[k] ? __fmul_rn(dk, sc[k]) : 0.f;
         }
         const bool small = nx <= 4 && ny <= 4 && nz <= 4;
-        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 4);
+        const unsigned dtab = dec + (unsigned)((((nx - 1) & 3) * 4 + ((ny - 1) & 3)) * 64 * 16);
         // box origin as floats (integers below 2^24: exact), its first cell
         const float fgx = (float)(ox + lx0), fgy = (float)(oy + ly0), fgz = (float)(oz + lz0);
         const int cell0 = (lz0 * Ty + ly0) * Tx + lx0;
@@ -511,9 +510,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             const int tt = rnd * 32 + lane;
             float4 d4;
             if (small) {  // warp-uniform; nround <= 2, so tt < 64
-                const unsigned c = lds_u32(dtab + 4u * (unsigned)tt);
-                d4 = make_float4((float)(c & 15u), (float)((c >> 4) & 15u), (float)((c >> 8) & 15u),
-                                 __int_as_float((int)(c >> 12)));
+                d4 = lds_f32x4(dtab + 16u * (unsigned)tt);
             } else {
                 const int ix = tt % nx, r = tt / nx, iy = r % ny, iz = r / ny;
                 d4 = make_float4((float)ix, (float)iy, (float)iz, __int_as_float((iz * Ty + iy) * Tx + ix));
