@@ -626,9 +626,10 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         if (tiles && tiles->bits) {
             auto lg = [](int v) { return (v & (v - 1)) == 0 ? __builtin_ctz((unsigned)v) : -1; };
             xm = XMask{tiles->bits, lg(tiles->tile[0]), lg(tiles->tile[1]), lg(tiles->tile[2]), tiles->ntile[0],
-                       tiles->ntile[1], G, (int)Gz};
+                       tiles->ntile[1], G, (int)Gz, FastDiv((unsigned)G), FastDiv((unsigned)Gz)};
             if (xm.sx < 0 || xm.sy < 0 || xm.sz < 0)
                 return fail(FR_ERR_UNSUPPORTED, "tile masks need power-of-two tile edges");
+            if (nl >= (1ll << 31)) return fail(FR_ERR_UNSUPPORTED, "more than 2^31 lines in a tile-masked transform");
         }
         rk->x<<<(unsigned)((nl + kRegLinesX - 1) / kRegLinesX), rk->xthreads, rk->xsmem, s>>>(grid, b1, nl, x0, rx, tw,
                                                                                           xm);

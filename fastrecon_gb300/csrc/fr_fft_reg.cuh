@@ -139,9 +139,30 @@ constexpr int kRegCols = 16;   // columns per CTA of the register column stages 
 // Cells the gridding left unwritten (tiles without samples) read as zero:
 // bit ((z >> sz) * nty + (y >> sy)) * ntx + (x >> sx) of `bits` is set for
 // written tiles (power-of-two tile edges; bits == nullptr: every cell).
+// n / d for n < 2^31 by a multiply and a shift: m = ceil(2^s / d) with
+// s = 31 + ceil(log2 d) leaves an error below 2^-ceil(log2 d) <= 1/d in
+// n * m / 2^s, too small to reach the next integer.
+struct FastDiv {
+    unsigned d = 1, m = 0x80000000u;
+    int s = 31;
+    FastDiv() = default;
+    explicit FastDiv(unsigned dd) : d(dd)
+    {
+        int l = 0;
+        while ((1ull << l) < dd) ++l;
+        s = 31 + l;
+        m = (unsigned)(((1ull << s) + dd - 1) / dd);
+    }
+    __device__ __forceinline__ unsigned div(unsigned n) const
+    {
+        return (unsigned)(((unsigned long long)n * m) >> s);
+    }
+};
+
 struct XMask {
     const unsigned *bits;
     int sx, sy, sz, ntx, nty, G, Gz;
+    FastDiv by_g, by_gz;  // line -> (y, z) without divisions
 };
 
 // x stage: kRegLinesX contiguous lines of length N per CTA, outputs
@@ -164,7 +185,9 @@ __global__ void __launch_bounds__(kRegLinesX * RegSplit<N>::TH) fft_x_kernel_reg
         const long long line = l0 + l;
         float2 v[M];
         if (line < nlines && xm.bits) {
-            const int y = (int)(line % xm.G), z = (int)((line / xm.G) % xm.Gz);
+            // nlines = coils * Gz * G < 2^31 (checked by the caller)
+            const unsigned yz = xm.by_g.div((unsigned)line), cz = xm.by_gz.div(yz);
+            const int y = (int)((unsigned)line - yz * (unsigned)xm.G), z = (int)(yz - cz * (unsigned)xm.Gz);
             const int tb = ((z >> xm.sz) * xm.nty + (y >> xm.sy)) * xm.ntx;
             const float2 *src = in + line * N + t;
 #pragma unroll
