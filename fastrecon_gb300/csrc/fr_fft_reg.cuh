@@ -247,12 +247,27 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     float2 *ex = tw + N;  // [k1][t][column]
+    // SoS: the next coil's input block [e][column], filled by cp.async while
+    // the current coil's second step runs (whole 16-byte column pairs only)
+    float2 *stage = ex + N * CB;
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
     const int cblocks = (ncols + CB - 1) / CB;
     const long long outer = blockIdx.x / cblocks;
     const int c0 = (blockIdx.x % cblocks) * CB;
     const int col = threadIdx.x % CB;
     const bool col_ok = c0 + col < ncols;
+    const bool pipe = SOS && ncols % CB == 0 && ((stride | in_outer_stride | cstride) & 1) == 0 &&
+                      (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    auto issue = [&](int coil) {
+        const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
+        for (int i = threadIdx.x; i < N * CB / 2; i += blockDim.x) {
+            const int e = i / (CB / 2), cc = 2 * (i % (CB / 2));
+            const unsigned dst = (unsigned)__cvta_generic_to_shared(stage + e * CB + cc);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src + (long long)e * stride + cc)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     float acc[SOS ? T : 1];
 #pragma unroll
     for (int k2 = 0; k2 < (SOS ? T : 1); ++k2) acc[k2] = 0.f;
@@ -267,14 +282,21 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
         }
     }
     const int ncoil = SOS ? coils : 1;
+    if (pipe) issue(0);
     for (int coil = 0; coil < ncoil; ++coil) {
-        __syncthreads();  // twiddles staged; the previous coil's exchange is read
+        if (pipe) asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();  // twiddles staged; the previous coil's exchange is read; this coil's block landed
         if (threadIdx.x < CB * T) {
             const int t = threadIdx.x / CB;
             float2 v[M];
-            const float2 *src = in + coil * cstride + outer * in_outer_stride + (long long)t * stride + c0 + col;
+            if (pipe) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) v[m] = col_ok ? src[(long long)(T * m) * stride] : make_float2(0.f, 0.f);
+                for (int m = 0; m < M; ++m) v[m] = stage[(t + T * m) * CB + col];
+            } else {
+                const float2 *src = in + coil * cstride + outer * in_outer_stride + (long long)t * stride + c0 + col;
+#pragma unroll
+                for (int m = 0; m < M; ++m) v[m] = col_ok ? src[(long long)(T * m) * stride] : make_float2(0.f, 0.f);
+            }
             rdft<M>(v);
             float2 *dst = ex + t * CB + col;
             dst[0] = v[0];
@@ -282,6 +304,7 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
             for (int k1 = 1; k1 < M; ++k1) dst[k1 * T * CB] = cmul(v[k1], tw[t * k1]);
         }
         __syncthreads();
+        if (pipe && coil + 1 < ncoil) issue(coil + 1);  // the block is free: every thread passed step A
         if (threadIdx.x < CB * M) {
             const int k1 = threadIdx.x / CB;
             float2 b[T];
@@ -332,4 +355,10 @@ template <int N>
 constexpr size_t reg_col_smem()
 {
     return (size_t)(N + N * kRegCols) * sizeof(float2);
+}
+// the SoS variant also holds the next coil's input block
+template <int N>
+constexpr size_t reg_col_sos_smem()
+{
+    return (size_t)(N + 2 * N * kRegCols) * sizeof(float2);
 }
