@@ -459,10 +459,12 @@ const CtKernels *ct_kernels(int n)
 
 // Register two-step stages (fr_fft_reg.cuh) for the specialised sizes.
 using FftXRegFn = void (*)(const float2 *, float2 *, long long, int, int, const float2 *, XMask);
+using FftColRegFn = void (*)(const float2 *, float2 *, int, int, int, long long, long long, long long, long long,
+                             const float2 *, int, long long, float *, const float *, int, int, long long);
 struct RegKernels {
     int n;
     FftXRegFn x;
-    FftColFn col, col_sos;
+    FftColRegFn col, col_sos;
     size_t xsmem, colsmem, colsossmem;
     int xthreads, colthreads;
 };
@@ -474,6 +476,8 @@ const RegKernels kRegKernels[] = {
     FR_REG(384), FR_REG(480), FR_REG(512), FR_REG(640),
 };
 #undef FR_REG
+
+constexpr int kColPer = 4;  // (coil, z) planes per CTA of the register y stage
 
 const RegKernels *reg_kernels(int n)
 {
@@ -618,8 +622,8 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         // register two-step stages: x (cropped), y (cropped), z or y with SoS
         if (rk->xsmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(rk->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->xsmem));
-        if (rk->colsmem > 48 * 1024)
-            FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
+        if (rk->colsossmem > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsossmem));
         if (rk->colsossmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(rk->col_sos, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)rk->colsossmem));
@@ -638,17 +642,20 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         const int cb = (rx + kRegCols - 1) / kRegCols;
         if (f->dim == 2) {
             rk->col_sos<<<cb, rk->colthreads, rk->colsossmem, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C,
-                                                            (long long)G * rx, d_out, d_deapod, sos_mode);
+                                                            (long long)G * rx, d_out, d_deapod, sos_mode, 1, 1);
             FR_CHECK_LAUNCH("fft_col_kernel_reg(y, sos)");
             return FR_OK;
         }
         float2 *b2 = f->b2.as<float2>();
-        rk->col<<<(unsigned)((long long)C * G * cb), rk->colthreads, rk->colsmem, s>>>(
-            b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0);
+        // y stage: kColPer consecutive (coil, z) planes per CTA
+        const long long nouter = (long long)C * G;
+        rk->col<<<(unsigned)((nouter + kColPer - 1) / kColPer * cb), rk->colthreads, rk->colsossmem, s>>>(
+            b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0, kColPer,
+            nouter);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(y)");
         rk->col_sos<<<(unsigned)((long long)ry * cb), rk->colthreads, rk->colsossmem, s>>>(
             b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C, (long long)G * ry * rx, d_out,
-            d_deapod, sos_mode);
+            d_deapod, sos_mode, 1, ry);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(z, sos)");
         return FR_OK;
     }

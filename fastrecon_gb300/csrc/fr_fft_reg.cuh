@@ -240,26 +240,30 @@ template <int N, bool SOS>
 __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) fft_col_kernel_reg(
     const float2 *__restrict__ in, float2 *__restrict__ out, int y0, int ry, int ncols, long long stride,
     long long in_outer_stride, long long out_outer_stride, long long out_stride, const float2 *__restrict__ tw_g,
-    int coils, long long cstride, float *__restrict__ sos_out, const float *__restrict__ deapod, int sos_mode)
+    int coils, long long cstride, float *__restrict__ sos_out, const float *__restrict__ deapod, int sos_mode,
+    int per, long long nouter)
 {
     constexpr int T = RegSplit<N>::T, M = RegSplit<N>::M;
     constexpr int CB = kRegCols;
     extern __shared__ float2 sm[];
     float2 *tw = sm;
     float2 *ex = tw + N;  // [k1][t][column]
-    // SoS: the next coil's input block [e][column], filled by cp.async while
-    // the current coil's second step runs (whole 16-byte column pairs only)
+    // The CTA's units, one after the other: with SOS the coils of one outer,
+    // else `per` consecutive outers of one coil.  The next unit's input block
+    // [e][column] is filled by cp.async while the current unit's second step
+    // runs (whole 16-byte column pairs only).
     float2 *stage = ex + N * CB;
     for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
     const int cblocks = (ncols + CB - 1) / CB;
-    const long long outer = blockIdx.x / cblocks;
+    const long long outer0 = SOS ? blockIdx.x / cblocks : (long long)(blockIdx.x / cblocks) * per;
+    const long long outer = outer0;  // the SoS outer
     const int c0 = (blockIdx.x % cblocks) * CB;
     const int col = threadIdx.x % CB;
     const bool col_ok = c0 + col < ncols;
-    const bool pipe = SOS && ncols % CB == 0 && ((stride | in_outer_stride | cstride) & 1) == 0 &&
+    const bool pipe = ncols % CB == 0 && ((stride | in_outer_stride | cstride) & 1) == 0 &&
                       (reinterpret_cast<uintptr_t>(in) & 15) == 0;
-    auto issue = [&](int coil) {
-        const float2 *src = in + coil * cstride + outer * in_outer_stride + c0;
+    auto issue = [&](int unit) {
+        const float2 *src = in + (SOS ? unit * cstride + outer0 * in_outer_stride : (outer0 + unit) * in_outer_stride) + c0;
         for (int i = threadIdx.x; i < N * CB / 2; i += blockDim.x) {
             const int e = i / (CB / 2), cc = 2 * (i % (CB / 2));
             const unsigned dst = (unsigned)__cvta_generic_to_shared(stage + e * CB + cc);
@@ -281,11 +285,13 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
             if (k >= y0 && k < y0 + ry) acc[k2] = o[(long long)(k - y0) * out_stride];
         }
     }
-    const int ncoil = SOS ? coils : 1;
+    const int nunit = SOS ? coils : (int)min((long long)per, nouter - outer0);
     if (pipe) issue(0);
-    for (int coil = 0; coil < ncoil; ++coil) {
+    for (int u = 0; u < nunit; ++u) {
+        const int coil = SOS ? u : 0;
+        const long long ou = SOS ? outer0 : outer0 + u;
         if (pipe) asm volatile("cp.async.wait_group 0;" ::: "memory");
-        __syncthreads();  // twiddles staged; the previous coil's exchange is read; this coil's block landed
+        __syncthreads();  // twiddles staged; the previous unit's exchange is read; this unit's block landed
         if (threadIdx.x < CB * T) {
             const int t = threadIdx.x / CB;
             float2 v[M];
@@ -293,7 +299,7 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
 #pragma unroll
                 for (int m = 0; m < M; ++m) v[m] = stage[(t + T * m) * CB + col];
             } else {
-                const float2 *src = in + coil * cstride + outer * in_outer_stride + (long long)t * stride + c0 + col;
+                const float2 *src = in + coil * cstride + ou * in_outer_stride + (long long)t * stride + c0 + col;
 #pragma unroll
                 for (int m = 0; m < M; ++m) v[m] = col_ok ? src[(long long)(T * m) * stride] : make_float2(0.f, 0.f);
             }
@@ -304,7 +310,7 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
             for (int k1 = 1; k1 < M; ++k1) dst[k1 * T * CB] = cmul(v[k1], tw[t * k1]);
         }
         __syncthreads();
-        if (pipe && coil + 1 < ncoil) issue(coil + 1);  // the block is free: every thread passed step A
+        if (pipe && u + 1 < nunit) issue(u + 1);  // the block is free: every thread passed step A
         if (threadIdx.x < CB * M) {
             const int k1 = threadIdx.x / CB;
             float2 b[T];
@@ -318,7 +324,7 @@ __global__ void __launch_bounds__(kRegCols * RegSplit<N>::TH, N <= 384 ? 2 : 1) 
                     // x * conj(x) of the reference's SOS: re*re - im*(-im)
                     acc[k2] = __fadd_rn(acc[k2], __fsub_rn(__fmul_rn(b[k2].x, b[k2].x), __fmul_rn(b[k2].y, -b[k2].y)));
             } else if (col_ok) {
-                float2 *o = out + outer * out_outer_stride + c0 + col;
+                float2 *o = out + ou * out_outer_stride + c0 + col;
 #pragma unroll
                 for (int k2 = 0; k2 < T; ++k2) {
                     const int k = k1 + M * k2;
@@ -356,7 +362,7 @@ constexpr size_t reg_col_smem()
 {
     return (size_t)(N + N * kRegCols) * sizeof(float2);
 }
-// the SoS variant also holds the next coil's input block
+// with the next unit's input block
 template <int N>
 constexpr size_t reg_col_sos_smem()
 {
