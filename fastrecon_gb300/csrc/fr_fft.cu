@@ -477,7 +477,7 @@ const RegKernels kRegKernels[] = {
 };
 #undef FR_REG
 
-constexpr int kColPer = 4;  // (coil, z) planes per CTA of the register y stage
+constexpr int kColPer = 8;  // (coil, z) planes per CTA of the register y stage
 
 const RegKernels *reg_kernels(int n)
 {

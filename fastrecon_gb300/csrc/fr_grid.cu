@@ -531,14 +531,13 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
             const int ex = (int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2));
             const unsigned m = __ballot_sync(0xffffffffu, ok);
             if (m == 0) continue;
-            // the list, padded to a multiple of four with weight-0 copies of
-            // the first entry (they add exactly 0 to a cell of this sample)
+            // the list, padded to a multiple of four with weight-0 entries on
+            // the tile's first cell row (they add exactly 0)
             const int n = __popc(m), n4 = (n + 3) & ~3;
-            const int e0x = __shfl_sync(0xffffffffu, ex, __ffs(m) - 1);
             const unsigned lst = mylist + buf * (kListEntries * 8);
             buf ^= 1;
             const int pos = ok ? __popc(m & lt) : n + __popc(~m & lt);
-            if (pos < n4) sts_s32x2(lst + 8u * (unsigned)pos, ok ? make_int2(ex, __float_as_int(w)) : make_int2(e0x, 0));
+            if (pos < n4) sts_s32x2(lst + 8u * (unsigned)pos, ok ? make_int2(ex, __float_as_int(w)) : make_int2((int)acc, 0));
             __syncwarp();
             // Entries hold the shared address of the tap's cell row; the tile
             // is 128-byte aligned, so the lane's swizzled float is address ^
