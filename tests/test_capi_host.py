@@ -72,6 +72,10 @@ def test_argument_validation_without_gpu(frlib):
     rd.dim = 2
     rd.channels = 0
     assert frlib.fr_recon_create(C.byref(rd), C.byref(h)) == 1
+    # host-buffer entry points: null handles and buffers are rejected up front
+    assert frlib.fr_recon_run_host(None, None, None, None, 0, None, None) == 1
+    assert frlib.fr_recon_submit_host(None, None, None, None, 0, None, None) == 1
+    assert frlib.fr_recon_sync(None, None) == 1
 
 
 def test_no_cpu_fallback_when_library_missing(tmp_path):
