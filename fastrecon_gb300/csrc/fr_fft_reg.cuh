@@ -175,9 +175,11 @@ __global__ void __launch_bounds__(kRegLinesX * RegSplit<N>::TH) fft_x_kernel_reg
     constexpr int T = RegSplit<N>::T, M = RegSplit<N>::M;
     constexpr int LS = M * (T + 1);  // [k1][t] with one pad slot per row
     extern __shared__ float2 sm[];
+    // twiddles of step A by (k1, t): tw[k1 T + t] = W^(t k1) (t k1 < T M = N),
+    // so the 16 lanes of a line read 16 consecutive entries
     float2 *tw = sm;
     float2 *ex = tw + N;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[i];
+    for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = tw_g[(i % T) * (i / T)];
     const long long l0 = (long long)blockIdx.x * kRegLinesX;
     __syncthreads();
     if (threadIdx.x < kRegLinesX * T) {
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(kRegLinesX * RegSplit<N>::TH) fft_x_kernel_reg
         float2 *dst = ex + l * LS + t;
         dst[0] = v[0];
 #pragma unroll
-        for (int k1 = 1; k1 < M; ++k1) dst[k1 * (T + 1)] = cmul(v[k1], tw[t * k1]);
+        for (int k1 = 1; k1 < M; ++k1) dst[k1 * (T + 1)] = cmul(v[k1], tw[k1 * T + t]);
     }
     __syncthreads();
     if (threadIdx.x < kRegLinesX * M) {
