@@ -465,12 +465,12 @@ struct RegKernels {
     int n;
     FftXRegFn x;
     FftColRegFn col, col_sos;
-    size_t xsmem, colsmem, colsossmem;
+    size_t xsmem, colsmem;
     int xthreads, colthreads;
 };
 #define FR_REG(N)                                                                                            \
     {N, fft_x_kernel_reg<N>, fft_col_kernel_reg<N, false>, fft_col_kernel_reg<N, true>, reg_x_smem<N>(),      \
-     reg_col_smem<N>(), reg_col_sos_smem<N>(), kRegLinesX * RegSplit<N>::TH, kRegCols * RegSplit<N>::TH}
+     reg_col_smem<N>(), kRegLinesX * RegSplit<N>::TH, kRegCols * RegSplit<N>::TH}
 const RegKernels kRegKernels[] = {
     FR_REG(64),  FR_REG(128), FR_REG(160), FR_REG(192), FR_REG(240), FR_REG(256), FR_REG(320),
     FR_REG(384), FR_REG(480), FR_REG(512), FR_REG(640),
@@ -622,11 +622,10 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         // register two-step stages: x (cropped), y (cropped), z or y with SoS
         if (rk->xsmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(rk->x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->xsmem));
-        if (rk->colsossmem > 48 * 1024)
-            FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsossmem));
-        if (rk->colsossmem > 48 * 1024)
-            FR_CUDA(cudaFuncSetAttribute(rk->col_sos, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)rk->colsossmem));
+        if (rk->colsmem > 48 * 1024) {
+            FR_CUDA(cudaFuncSetAttribute(rk->col, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
+            FR_CUDA(cudaFuncSetAttribute(rk->col_sos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rk->colsmem));
+        }
         XMask xm{};
         if (tiles && tiles->bits) {
             auto lg = [](int v) { return (v & (v - 1)) == 0 ? __builtin_ctz((unsigned)v) : -1; };
@@ -641,7 +640,7 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         FR_CHECK_LAUNCH("fft_x_kernel_reg");
         const int cb = (rx + kRegCols - 1) / kRegCols;
         if (f->dim == 2) {
-            rk->col_sos<<<cb, rk->colthreads, rk->colsossmem, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C,
+            rk->col_sos<<<cb, rk->colthreads, rk->colsmem, s>>>(b1, nullptr, y0, ry, rx, rx, 0, 0, rx, tw, C,
                                                             (long long)G * rx, d_out, d_deapod, sos_mode, 1, 1);
             FR_CHECK_LAUNCH("fft_col_kernel_reg(y, sos)");
             return FR_OK;
@@ -649,11 +648,11 @@ int fftcs_execute(fr_fftcs f, const float *d_grid, int channels, const float *d_
         float2 *b2 = f->b2.as<float2>();
         // y stage: kColPer consecutive (coil, z) planes per CTA
         const long long nouter = (long long)C * G;
-        rk->col<<<(unsigned)((nouter + kColPer - 1) / kColPer * cb), rk->colthreads, rk->colsossmem, s>>>(
+        rk->col<<<(unsigned)((nouter + kColPer - 1) / kColPer * cb), rk->colthreads, rk->colsmem, s>>>(
             b1, b2, y0, ry, rx, rx, (long long)G * rx, (long long)ry * rx, rx, tw, 1, 0, nullptr, nullptr, 0, kColPer,
             nouter);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(y)");
-        rk->col_sos<<<(unsigned)((long long)ry * cb), rk->colthreads, rk->colsossmem, s>>>(
+        rk->col_sos<<<(unsigned)((long long)ry * cb), rk->colthreads, rk->colsmem, s>>>(
             b2, nullptr, z0, rz, rx, (long long)ry * rx, rx, rx, (long long)ry * rx, tw, C, (long long)G * ry * rx, d_out,
             d_deapod, sos_mode, 1, ry);
         FR_CHECK_LAUNCH("fft_col_kernel_reg(z, sos)");

@@ -359,14 +359,9 @@ constexpr size_t reg_x_smem()
 {
     return (size_t)(N + kRegLinesX * RegSplit<N>::M * (RegSplit<N>::T + 1)) * sizeof(float2);
 }
+// twiddles, exchange buffer and the next unit's input block
 template <int N>
 constexpr size_t reg_col_smem()
-{
-    return (size_t)(N + N * kRegCols) * sizeof(float2);
-}
-// with the next unit's input block
-template <int N>
-constexpr size_t reg_col_sos_smem()
 {
     return (size_t)(N + 2 * N * kRegCols) * sizeof(float2);
 }
