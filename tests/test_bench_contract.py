@@ -45,3 +45,16 @@ def test_reference_arm_under_torchrun_two_ranks():
     lines = _lines(r.stdout)
     assert len(lines) == 1  # rank 0 alone
     _check(lines[0], 2)
+
+
+def test_gpu_arm_has_no_cpu_fallback():
+    """Without a GPU the measured arm exits non-zero and prints no result
+    line: nothing is timed on a CPU stand-in."""
+    import pytest
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = subprocess.run([sys.executable, "bench.py", "--workload", "radial2d", "--steps", "1", "--warmup", "0"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0
+    assert not _lines(r.stdout)
