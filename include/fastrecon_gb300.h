@@ -393,6 +393,10 @@ typedef struct {
                                 channels x G^d x 8 to slab x G^d x 8 bytes */
 } fr_recon_desc;
 
+/* One fr_recon object holds one plan and one grid workspace: give all its
+ * calls the same stream (calls on other streams or host threads race), or
+ * use one object per stream.  fr_recon_destroy waits for its submitted
+ * volumes. */
 int fr_recon_create(const fr_recon_desc *desc, fr_recon *out);
 int fr_recon_destroy(fr_recon r);
 /* Device buffers: d_traj n x 4 raw coordinates, d_dcf n, d_kdata channels x n
