@@ -166,15 +166,17 @@ void orc_lut_index_of_s(const float *s, size_t n, float kHW, int klength, int *o
     }
 }
 
-/* GridLut::griddingChannel, GridLut.cpp:80-147. */
-void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, size_t n,
-                      int dim, unsigned G, float kWidth, const float *lut, int klength,
-                      float *out)
+/* GridLut::griddingChannel, GridLut.cpp:80-147, restricted to the cells of
+ * the last axis (z in 3D, y in 2D) in [b0, b1): every sample is visited in
+ * sample order and only its taps inside the band are added, so each cell of
+ * the band receives exactly the adds of the full loop, in the same order.
+ * The band is not cleared here. */
+static void grid_channel_band(const float *traj, const float *dcf, const float *kdata, size_t n,
+                              int dim, unsigned G, float kWidth, const float *lut, int klength,
+                              float *out, int b0, int b1)
 {
     float kHW = kWidth / 2;
-    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
-    memset(out, 0, cells * 2 * sizeof(float));
-
+    const int last = dim - 1;
     for (size_t s = 0; s < n; ++s) {
         float center[3] = {0, 0, 0};
         int start[3] = {0, 0, 0}, end[3] = {0, 0, 0};
@@ -182,6 +184,12 @@ void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, s
             center[i] = traj[4 * s + i];
             comp_range(center[i], kHW, G, &start[i], &end[i]);
         }
+        if (start[last] < b0)
+            start[last] = b0;
+        if (end[last] > b1 - 1)
+            end[last] = b1 - 1;
+        if (start[last] > end[last])
+            continue;
         /* GridLut.cpp:109: data = dcf * sample (complex<float> times float). */
         float dre = dcf[s] * kdata[2 * s];
         float dim_ = dcf[s] * kdata[2 * s + 1];
@@ -210,6 +218,40 @@ void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, s
     }
 }
 
+/* GridLut::griddingChannel, GridLut.cpp:80-147. */
+void orc_grid_channel(const float *traj, const float *dcf, const float *kdata, size_t n,
+                      int dim, unsigned G, float kWidth, const float *lut, int klength,
+                      float *out)
+{
+    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
+    memset(out, 0, cells * 2 * sizeof(float));
+    grid_channel_band(traj, dcf, kdata, n, dim, G, kWidth, lut, klength, out, 0, (int)G);
+}
+
+void orc_grid_bands(const float *traj, const float *dcf, const float *kdata, size_t n,
+                    int channels, int dim, unsigned G, float kWidth, const float *lut,
+                    int klength, float *out, int threads)
+{
+    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
+    size_t band_cells = cells / G; /* cells per z (3D) or y (2D) index */
+    if (threads < 1)
+        threads = 1;
+    int nb = threads * 4;
+    if (nb > (int)G)
+        nb = (int)G;
+    (void)threads;
+    for (int c = 0; c < channels; ++c) {
+        float *o = out + 2 * (size_t)c * cells;
+        const float *kd = kdata + 2 * (size_t)c * n;
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+        for (int b = 0; b < nb; ++b) {
+            int b0 = (int)((long long)G * b / nb), b1 = (int)((long long)G * (b + 1) / nb);
+            memset(o + 2 * (size_t)b0 * band_cells, 0, (size_t)(b1 - b0) * band_cells * 2 * sizeof(float));
+            grid_channel_band(traj, dcf, kd, n, dim, G, kWidth, lut, klength, o, b0, b1);
+        }
+    }
+}
+
 /* GridLut::execute, GridLut.cpp:53-78. */
 void orc_grid(const float *traj, const float *dcf, const float *kdata, size_t n,
               int channels, int dim, unsigned G, float kWidth, const float *lut,
@@ -225,13 +267,12 @@ void orc_grid(const float *traj, const float *dcf, const float *kdata, size_t n,
                          out + 2 * (size_t)c * cells);
 }
 
-void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdata, size_t n,
-                          int dim, unsigned G, float kWidth, const float *lut, int klength,
-                          double *out)
+static void grid_channel_band_f64(const float *traj, const float *dcf, const float *kdata, size_t n,
+                                  int dim, unsigned G, float kWidth, const float *lut, int klength,
+                                  double *out, int b0, int b1)
 {
     float kHW = kWidth / 2;
-    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
-    memset(out, 0, cells * 2 * sizeof(double));
+    const int last = dim - 1;
     for (size_t s = 0; s < n; ++s) {
         float center[3] = {0, 0, 0};
         int start[3] = {0, 0, 0}, end[3] = {0, 0, 0};
@@ -239,6 +280,12 @@ void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdat
             center[i] = traj[4 * s + i];
             comp_range(center[i], kHW, G, &start[i], &end[i]);
         }
+        if (start[last] < b0)
+            start[last] = b0;
+        if (end[last] > b1 - 1)
+            end[last] = b1 - 1;
+        if (start[last] > end[last])
+            continue;
         double dre = (double)dcf[s] * (double)kdata[2 * s];
         double dimg = (double)dcf[s] * (double)kdata[2 * s + 1];
         for (int z = start[2]; z <= end[2]; z++) {
@@ -254,6 +301,39 @@ void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdat
                     }
                 }
             }
+        }
+    }
+}
+
+void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdata, size_t n,
+                          int dim, unsigned G, float kWidth, const float *lut, int klength,
+                          double *out)
+{
+    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
+    memset(out, 0, cells * 2 * sizeof(double));
+    grid_channel_band_f64(traj, dcf, kdata, n, dim, G, kWidth, lut, klength, out, 0, (int)G);
+}
+
+void orc_grid_f64_bands(const float *traj, const float *dcf, const float *kdata, size_t n,
+                        int channels, int dim, unsigned G, float kWidth, const float *lut,
+                        int klength, double *out, int threads)
+{
+    size_t cells = (dim == 3) ? (size_t)G * G * G : (size_t)G * G;
+    size_t band_cells = cells / G;
+    if (threads < 1)
+        threads = 1;
+    int nb = threads * 4;
+    if (nb > (int)G)
+        nb = (int)G;
+    (void)threads;
+    for (int c = 0; c < channels; ++c) {
+        double *o = out + 2 * (size_t)c * cells;
+        const float *kd = kdata + 2 * (size_t)c * n;
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+        for (int b = 0; b < nb; ++b) {
+            int b0 = (int)((long long)G * b / nb), b1 = (int)((long long)G * (b + 1) / nb);
+            memset(o + 2 * (size_t)b0 * band_cells, 0, (size_t)(b1 - b0) * band_cells * 2 * sizeof(double));
+            grid_channel_band_f64(traj, dcf, kd, n, dim, G, kWidth, lut, klength, o, b0, b1);
         }
     }
 }

@@ -80,6 +80,22 @@ void orc_grid_channel_f64(const float *traj, const float *dcf, const float *kdat
                           int dim, unsigned G, float kWidth, const float *lut, int klength,
                           double *out);
 
+/* orc_grid with each channel split over `threads` threads by bands of the
+ * last grid axis (z in 3D, y in 2D) instead of one thread per channel: every
+ * thread walks all samples in sample order and adds only the taps inside its
+ * band, so every cell gets the reference's adds in the reference's order and
+ * the result is bit-for-bit that of orc_grid.  For full-size checks. */
+void orc_grid_bands(const float *traj, const float *dcf, const float *kdata, size_t n,
+                    int channels, int dim, unsigned G, float kWidth, const float *lut,
+                    int klength, float *out, int threads);
+
+/* The FP64 gridding oracle for all channels, split into bands the same way
+ * (bit-for-bit orc_grid_channel_f64 per channel).  out: channels*G^d complex
+ * double. */
+void orc_grid_f64_bands(const float *traj, const float *dcf, const float *kdata, size_t n,
+                        int channels, int dim, unsigned G, float kWidth, const float *lut,
+                        int klength, double *out, int threads);
+
 /* Per-sample kernel mass: sum over the sample's valid taps of lut[ki], with
  * the reference geometry (GridLut.cpp:98-136), in double.  Gridding is
  * linear, so sum_cells grid[c] = sum_s dcf[s]*kdata[c][s]*mass[s]: a

@@ -48,6 +48,25 @@ def test_recon_bit_exact(oracle, case):
     assert np.array_equal(bits(img), bits(case["image"]))
 
 
+def test_band_split_oracle_bit_exact(oracle, case):
+    """The band-parallel gridding used for full-size checks gives the golden
+    (reference-built) grid and image bit for bit, and the band-parallel FP64
+    oracle equals the sequential one."""
+    tn = case["traj_norm"]
+    for threads in (1, 3, 8):
+        g = oracle.grid_bands(tn, case["dcf"], case["kdata"], case["dim"], case["G"], case["W"], case["lut"],
+                              threads=threads)
+        assert np.array_equal(bits(g.view(np.float32)), bits(case["grid"].view(np.float32))), threads
+    rec = (case["recon"],) * 2 + ((case["recon"] if case["dim"] == 3 else 1),)
+    img = oracle.recon_bands(case["traj"], case["dcf"], case["kdata"], case["dim"], case["recon"], case["os"],
+                             case["W"], case["L"], rec, threads=5)
+    assert np.array_equal(bits(img), bits(case["image"]))
+    g64 = oracle.grid_f64(tn, case["dcf"], case["kdata"], case["dim"], case["G"], case["W"], case["lut"])
+    g64b = oracle.grid_f64_bands(tn, case["dcf"], case["kdata"], case["dim"], case["G"], case["W"], case["lut"],
+                                 threads=7)
+    assert np.array_equal(g64, g64b)
+
+
 def test_fp64_oracle_close(oracle, case):
     """The FP32 reference grid vs the FP64 oracle: the reference's own
     rounding error, stated per fixture."""
