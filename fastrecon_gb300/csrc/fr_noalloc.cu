@@ -10,8 +10,9 @@
 //
 // The scratch is a file-scope __device__ array of FR_NOALLOC_SCRATCH_BYTES
 // (32 MiB): every GPU that loads this library holds it until the process
-// exits.  Its device address is looked up with cudaGetSymbolAddress the first
-// time the entry point runs on a device (with that device current); the
+// exits.  Its device address is looked up with cudaGetSymbolAddress on every
+// call, on the caller's current device (a host-side query; nothing is cached,
+// so a device reset or a reloaded module never leaves a stale address); the
 // address of the array's name in host code is only a host-side stand-in and
 // is never passed to a kernel.  All calls share the array and it keeps the
 // last call's contents: the counters that must start at zero are cleared by
@@ -21,7 +22,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 
 #include "fr_internal.h"
 
@@ -30,25 +30,13 @@ namespace {
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[FR_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-unsigned char *g_scratch_dev[kMaxDevices] = {};
-
-// Device address of the scratch on the current device (looked up once per device).
+// Device address of the scratch on the current device.
 int scratch_on_current_device(unsigned char **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices) return fail(FR_ERR_UNSUPPORTED, "device index above 63");
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_dev[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
-        g_scratch_dev[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_scratch_dev[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-allocation scratch)");
+    *out = static_cast<unsigned char *>(p);
     return FR_OK;
 }
 

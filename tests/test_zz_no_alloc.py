@@ -63,3 +63,64 @@ def test_noalloc_matches_plan_and_grid(frlib, name):
     for got in outs:
         assert rel_l2(got, want) <= TOL
         assert rel_l2(got, c["grid"]) <= TOL
+
+
+def _noalloc(frlib, torch, traj, dim, G, W, lut, kd, dcf, coils):
+    lut = np.ascontiguousarray(lut, np.float32)
+    out = torch.full((coils, G ** dim), float("nan"), dtype=torch.complex64, device="cuda")
+    st = frlib.fr_grid_noalloc(C.c_void_p(traj.data_ptr()), traj.shape[0], dim, G, W,
+                               lut.ctypes.data_as(C.POINTER(C.c_float)), len(lut), C.c_void_p(kd.data_ptr()),
+                               C.c_void_p(dcf.data_ptr()), coils, C.c_void_p(out.data_ptr()),
+                               C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    return st, out
+
+
+def _golden_call(frlib, torch, name):
+    c = load_case(name)
+    st, out = _noalloc(frlib, torch, torch.from_numpy(c["traj"]).cuda(), c["dim"], c["G"], c["W"], c["lut"],
+                       torch.from_numpy(c["kdata"]).cuda(), torch.from_numpy(c["dcf"]).cuda(), c["coils"])
+    assert st == 0, frlib.fr_last_error()
+    return rel_l2(out.cpu().numpy(), c["grid"])
+
+
+@pytest.mark.gpu
+def test_noalloc_alternating_cases(frlib):
+    """Calls with different trajectories in a row -- a larger 3D case, a
+    smaller 2D one on an odd grid, the 3D one again -- each match the
+    reference's grid: counters, tile tables and partial tiles left by the
+    call before do not leak into the next."""
+    import torch
+    for name in ["koosh3d_small", "radial2d_oddgrid", "koosh3d_small", "radial2d_small", "koosh3d_odd"]:
+        assert _golden_call(frlib, torch, name) <= TOL, name
+
+
+@pytest.mark.gpu
+def test_noalloc_capacity_found_after_planning(frlib):
+    """Trajectories whose bin records (a 3D kooshball of 1 M samples on a 64^3
+    grid) or split-tile partials (200,000 samples at one point of a 2D grid)
+    exceed the scratch are counted by the plan's kernels and then refused
+    with FR_ERR_CAPACITY; the next call with a good trajectory is correct."""
+    import torch
+
+    from fastrecon_gb300 import synth
+    lut = load_case("koosh3d_small")["lut"]
+    traj = synth.kooshball_3d(4000, 256)
+    n = traj.shape[0]
+    t = torch.from_numpy(traj).cuda()
+    kd = torch.ones((1, n), dtype=torch.complex64, device="cuda")
+    dcf = torch.ones(n, dtype=torch.float32, device="cuda")
+    st, _ = _noalloc(frlib, torch, t, 3, 64, 4.0, lut, kd, dcf, 1)
+    assert st == 9 and b"bin lists" in frlib.fr_last_error(), frlib.fr_last_error()
+    assert _golden_call(frlib, torch, "koosh3d_small") <= TOL
+
+    m = 200_000
+    pts = np.zeros((m, 4), np.float32)
+    pts[0, :2] = -0.5
+    pts[1, :2] = 0.4999
+    t = torch.from_numpy(pts).cuda()
+    kd = torch.ones((8, m), dtype=torch.complex64, device="cuda")
+    dcf = torch.ones(m, dtype=torch.float32, device="cuda")
+    st, _ = _noalloc(frlib, torch, t, 2, 512, 4.0, load_case("radial2d_small")["lut"], kd, dcf, 8)
+    assert st == 9 and b"partial tiles" in frlib.fr_last_error(), frlib.fr_last_error()
+    assert _golden_call(frlib, torch, "radial2d_small") <= TOL
