@@ -14,6 +14,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "libfastrecon_gb300.so")
 
 FR_PLAN_CHECKERBOARD = 1
+FR_PLAN_NO_TAP_LISTS = 4
 FR_RECON_DEAPODIZE = 1
 FR_RECON_CUFFT = 2
 FR_RECON_PRUNED_FFT = 4
@@ -58,6 +59,7 @@ _SIGS = {
     "fr_plan_stats": (C.c_int, [_VP, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                 C.POINTER(C.c_longlong)]),
     "fr_plan_bins": (C.c_int, [_VP, _VP, _VP, _VP]),
+    "fr_plan_tap_words": (C.c_int, [_VP, C.POINTER(C.c_int)]),
     "fr_plan_profile": (C.c_int, [_VP, C.c_int]),
     "fr_plan_profile_read": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "fr_kernel_launches": (C.c_longlong, []),

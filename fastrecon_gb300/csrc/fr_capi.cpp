@@ -158,6 +158,7 @@ void lut_index_table_into(float hw, int L, float *thr, float *smax, float *kc)
 fr_plan_s::~fr_plan_s()
 {
     for (auto e : prof_ev) cudaEventDestroy(e);
+    if (err_host) cudaFreeHost(err_host);
 }
 
 using namespace fr;
@@ -277,6 +278,7 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
     {
         const char *cm = std::getenv("FR_KSPACE_COIL_MAJOR");
         p->kspace_sample_major = !(cm && std::atoi(cm) != 0);
+        p->taps_enabled = !(d->flags & FR_PLAN_NO_TAP_LISTS);
     }
     {
         // exact when hw^2 is representable and sqrt rounds back to hw
@@ -310,6 +312,14 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         delete p;
         return cuda_fail(e, "lut upload");
     }
+    // a word the kernels set on an internal error, read by the host without a copy
+    e = cudaHostAlloc(reinterpret_cast<void **>(&p->err_host), sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&p->err_dev), p->err_host, 0);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "error word");
+    }
+    *p->err_host = 0;
     *out = p;
     return FR_OK;
 }
@@ -362,6 +372,13 @@ int fr_plan_stats(fr_plan p, long long *tiles, long long *pairs, long long *item
     if (pairs) *pairs = p->npairs;
     if (items) *items = p->nitems;
     if (slots) *slots = p->nslots;
+    return FR_OK;
+}
+
+int fr_plan_tap_words(fr_plan p, int *words)
+{
+    if (!p || !words) return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    *words = p->planned ? p->tap_words : 0;
     return FR_OK;
 }
 

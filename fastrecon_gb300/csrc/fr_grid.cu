@@ -61,6 +61,14 @@ struct GridParams {
     // per-item scale then needs one float per record
     const float *mag;
     int skip_empty;     // tiles without samples are left unwritten
+    // tap lists (grid_taps_kernel): per record sample | first word << 32 |
+    // taps << 40, per sample a slot of tap_words tap words
+    const unsigned long long *trecs = nullptr;
+    const unsigned *taps = nullptr;
+    const float *lutw = nullptr;        // L weights
+    const float *item_inv = nullptr;    // per work item: inverse fixed-point scale
+    int tap_words = 0;
+    long long kstride = 0;    // complex values per sample row of the sample-major k-space
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -120,6 +128,12 @@ __device__ __forceinline__ unsigned lds_u32(unsigned a)
 {
     unsigned r;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
+    return r;
+}
+__device__ __forceinline__ float lds_f32(unsigned a)
+{
+    float r;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(a) : "memory");
     return r;
 }
 __device__ __forceinline__ float4 lds_f32x4(unsigned a)
@@ -445,7 +459,7 @@ __device__ __forceinline__ void grid_item(const GridParams &P, const WorkItem &i
     const float *kdf[NF];
     bool coil_ok[NF];
     lane_kspace<NF>(P, cg, f0, s_off, n_f, kdf, coil_ok);
-    const size_t ks = P.sample_major ? 2 * (size_t)P.channels : 2;
+    const size_t ks = P.sample_major ? 2 * (size_t)P.kstride : 2;
     const unsigned long long *recs = P.recs + it.begin;
 
     if (P.mag) {
@@ -629,6 +643,225 @@ __global__ void __launch_bounds__(512) grid_persistent_kernel(GridParams P)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Scatter from the plan's tap lists.
+//
+// The geometry of every tap was evaluated once per trajectory by the plan,
+// so per bin record the CTA only moves data and accumulates.  Each warp
+// walks its share of the work item's records with the loads of kTapDepth
+// records in flight: for record k + kTapDepth, lane t loads the record's tap
+// word t (t + 32) and lane f its coil float f of the record's dcf * k values
+// into registers while record k is accumulated.  Lanes decode the taps
+// into the warp's list {shared address of the tap's cell row, weight}, and
+// lanes mapped to coil floats add round(w * v * S) into the fixed-point
+// tile as grid_item does.
+// ---------------------------------------------------------------------------
+constexpr int kTapDepth = 4;   // records in flight per warp
+constexpr int kTapList = 64;   // list entries per warp (records hold <= kTapRecMax taps, padded)
+
+// Shared-memory layout of grid_taps_kernel, from its 128-byte aligned base:
+// tile [K][R] int32 | inverse scales [R] (256 B) | weights [L] | per warp a
+// list [kTapList] {address, weight}.
+struct TapSmem {
+    unsigned inv, lutw, lists, end;
+};
+__host__ __device__ __forceinline__ TapSmem tap_smem_layout(long long K, int R, int L)
+{
+    TapSmem m;
+    m.inv = (unsigned)(K * R * 4);
+    m.lutw = m.inv + 256u;
+    m.lists = m.lutw + (unsigned)((L * 4 + 15) & ~15);
+    m.end = m.lists + (unsigned)(kWarps * kTapList * 8);
+    return m;
+}
+
+// One record's data in flight: its tap count, the lane's tap words and the
+// lane's coil float.
+struct TapStage {
+    int nt;
+    unsigned t0, t1;
+    float v;
+};
+
+template <int R>
+__global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
+{
+    extern __shared__ float4 smem_raw[];
+    float4 *smem4 = aligned_smem(smem_raw);
+    const WorkItem it = P.items[blockIdx.x];
+    const int cg = blockIdx.y;
+    const int K = P.K;
+    const int CG = P.coil_group;
+    const TapSmem L_ = tap_smem_layout(K, R, P.L);
+    const unsigned acc = smem_addr(smem4);
+    float *inv_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + L_.inv);
+    float *lutw_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + L_.lutw);
+
+    const int t = it.tile;
+    const int ox = (t % P.ntile[0]) * P.tile[0];
+    const int oy = ((t / P.ntile[0]) % P.ntile[1]) * P.tile[1];
+    const int oz = (t / (P.ntile[0] * P.ntile[1])) * P.tile[2];
+
+    if (it.count == 0) {
+        if (!P.skip_empty) write_cell_group<R>(P, P.grid, acc, cg, ox, oy, oz, true, inv_s);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const unsigned list = acc + L_.lists + (unsigned)(warp * kTapList * 8);
+
+    for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutw_s[i] = P.lutw[i];
+    const float inv = P.item_inv[blockIdx.x];
+    if (threadIdx.x < R) inv_s[threadIdx.x] = inv;
+    __syncthreads();
+
+    constexpr int NG = R >= 32 ? 1 : 32 / R;  // taps per accumulate step
+    constexpr int PAD = NG > 2 ? NG : 2;      // list length granularity
+    const int q = R >= 32 ? 0 : lane / R;     // tap slot of this lane
+    const int f0 = R >= 32 ? lane : lane % R; // coil float of this lane
+    const unsigned f0b = (unsigned)f0 << 2;
+    const float sc = __fdiv_rn(1.f, inv);     // exact: a power of two
+    const int ncl = min(CG, P.channels - cg * CG);
+    const bool vlane = (f0 >> 1) < ncl;
+    const float *kt = P.kdata + 2 * (size_t)cg * CG + f0;
+    const unsigned *taps = P.taps;
+    const size_t tw = (size_t)P.tap_words;
+
+    // the warp's records: batches of 32 consecutive records, batch b = warp,
+    // warp + kWarps, ...; record k of the warp is lane k % 32 of its batch
+    // k / 32.  Record words past the item read as 0 (no taps).
+    const int nb = (it.count + 31) >> 5;
+    const int nbw = warp < nb ? (nb - warp + kWarps - 1) / kWarps : 0;
+    const int nrec = nbw * 32;
+    const unsigned long long *trecs = P.trecs + it.begin;
+    auto batch_word = [&](int i) -> unsigned long long {
+        const int j = 32 * (warp + kWarps * i) + lane;
+        return i < nbw && j < it.count ? __ldg(trecs + j) : 0ull;
+    };
+    auto fetch = [&](unsigned long long rw, TapStage &st) {
+        st.nt = (int)((rw >> 40) & 0xFF);
+        const size_t base = (size_t)(unsigned)rw * tw + (size_t)((rw >> 32) & 0xFF);
+        st.t0 = lane < st.nt ? __ldg(taps + base + lane) : 0u;
+        st.t1 = lane + 32 < st.nt ? __ldg(taps + base + lane + 32) : 0u;
+        st.v = vlane && st.nt ? __ldg(kt + 2 * (size_t)(unsigned)rw * (size_t)P.kstride) : 0.f;
+    };
+
+    unsigned long long cur = batch_word(0), nxt = batch_word(1);
+    TapStage st[kTapDepth];
+#pragma unroll
+    for (int d = 0; d < kTapDepth; ++d) fetch(__shfl_sync(0xffffffffu, cur, d), st[d]);
+
+    for (int k0 = 0; k0 < nrec; k0 += kTapDepth) {
+        if (k0 > 0 && (k0 & 31) == 0) {
+            cur = nxt;
+            nxt = batch_word((k0 >> 5) + 1);
+        }
+#pragma unroll
+        for (int d = 0; d < kTapDepth; ++d) {
+            const int k = k0 + d;
+            const int ntap = st[d].nt;
+            const int np = (ntap + PAD - 1) / PAD * PAD;
+            const float vs = __fmul_rn(st[d].v, sc);
+            if (ntap > 0) {
+                // decode: list entry i = {address of tap i's cell row, weight};
+                // pad entries add 0 to the first cell row
+                int2 e = make_int2((int)acc, 0);
+                if (lane < ntap) {
+                    const int cell = (int)(st[d].t0 & ((1u << kTapCellBits) - 1u));
+                    e.x = (int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2));
+                    e.y = __float_as_int(lds_f32(acc + L_.lutw + 4u * (st[d].t0 >> kTapCellBits)));
+                }
+                if (lane < np) sts_s32x2(list + 8u * (unsigned)lane, e);
+                if (np > 32) {
+                    int2 e1 = make_int2((int)acc, 0);
+                    if (lane + 32 < ntap) {
+                        const int cell = (int)(st[d].t1 & ((1u << kTapCellBits) - 1u));
+                        e1.x = (int)(acc + ((unsigned)(cell * R + swz<R>(cell)) << 2));
+                        e1.y = __float_as_int(lds_f32(acc + L_.lutw + 4u * (st[d].t1 >> kTapCellBits)));
+                    }
+                    if (lane + 32 < np) sts_s32x2(list + 8u * (unsigned)(lane + 32), e1);
+                }
+            }
+            __syncwarp();
+            // refill this stage with record k + kTapDepth
+            const int k2 = k + kTapDepth;
+            if (k2 < nrec) {
+                const unsigned long long src = (k2 >> 5) == (k0 >> 5) ? cur : nxt;
+                fetch(__shfl_sync(0xffffffffu, src, k2 & 31), st[d]);
+            } else {
+                st[d].nt = 0;
+            }
+            if (ntap > 0) {
+                if (NG == 1) {
+                    for (int m = 0; m < np; m += 2) {
+                        const int4 e = lds_s32x4(list + 8u * (unsigned)m);
+                        red_add_fx((unsigned)e.x ^ f0b, __int_as_float(e.y), vs);
+                        red_add_fx((unsigned)e.z ^ f0b, __int_as_float(e.w), vs);
+                    }
+                } else {
+                    for (int m = q; m < np; m += NG) {
+                        const int2 e = lds_s32x2(list + 8u * (unsigned)m);
+                        red_add_fx((unsigned)e.x ^ f0b, __int_as_float(e.y), vs);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    if (it.slot < 0) {
+        write_cell_group<R>(P, P.grid, acc, cg, ox, oy, oz, false, inv_s);
+    } else {
+        float4 *dst = reinterpret_cast<float4 *>(P.partials + ((size_t)it.slot * P.ngroups + cg) * (size_t)K * R);
+        const int4 *src = reinterpret_cast<const int4 *>(smem4);
+        for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) {
+            const int4 a = src[i];
+            dst[i] = make_float4((float)a.x * inv, (float)a.y * inv, (float)a.z * inv, (float)a.w * inv);
+        }
+    }
+}
+
+// Per work item, from the per-sample bounds (mag[s] >= every |dcf * k| of
+// sample s), one warp per item: the sum and the maximum over the item's
+// records with taps.
+__global__ void item_bound_kernel(const WorkItem *__restrict__ items, long long nitems,
+                                  const unsigned long long *__restrict__ trecs, const float *__restrict__ mag,
+                                  float2 *__restrict__ bound)
+{
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nitems) return;
+    const WorkItem it = items[w];
+    float bs = 0.f, bm = 0.f;
+    for (int j = lane; j < it.count; j += 32) {
+        const unsigned long long rw = trecs[it.begin + j];
+        if ((rw >> 40) & 0xFF) {
+            const float a = mag[(unsigned)rw];
+            bs += a;
+            bm = fmaxf(bm, a);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bs += __shfl_xor_sync(0xffffffffu, bs, o);
+        bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+    }
+    if (lane == 0) bound[w] = make_float2(bs, bm);
+}
+
+// Inverse fixed-point scale of every work item from its own bound (see
+// inv_scale_of).
+__global__ void item_inv_kernel(const float2 *__restrict__ bound, long long nitems, float lut_absmax,
+                                float *__restrict__ inv)
+{
+    for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nitems;
+         w += (long long)gridDim.x * blockDim.x) {
+        const float2 b = bound[w];
+        inv[w] = inv_scale_of(b.x, __float_as_uint(b.y), lut_absmax);
+    }
+}
+
 // Sum the partial tiles of each split tile in item order and write the grid.
 // CTA (split tile, coil group, part): part z of kReduceParts holds a run of
 // the tile's rows.  The partial rows are read as contiguous float4 ([cell][R]
@@ -743,7 +976,7 @@ __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const floa
                                                                       const float *__restrict__ dcf,
                                                                       float2 *__restrict__ out,
                                                                       float *__restrict__ mag, long long n,
-                                                                      int channels)
+                                                                      int channels, int cstride)
 {
     extern __shared__ float2 tr[];  // [channels][kTrSamples + 1]
     __shared__ float dsh[kTrSamples];
@@ -766,11 +999,16 @@ __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const floa
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < channels * ns; i += kTrThreads) {
-        const int j = i / channels, c = i - j * channels;
-        const float2 v = tr[c * (kTrSamples + 1) + j];
-        const float d = dsh[j];
-        out[(size_t)(s0 + j) * channels + c] = make_float2(__fmul_rn(d, v.x), __fmul_rn(d, v.y));
+    // rows of cstride >= channels complex values (the pad, if any, is zero)
+    for (int i = threadIdx.x; i < cstride * ns; i += kTrThreads) {
+        const int j = i / cstride, c = i - j * cstride;
+        float2 o = make_float2(0.f, 0.f);
+        if (c < channels) {
+            const float2 v = tr[c * (kTrSamples + 1) + j];
+            const float d = dsh[j];
+            o = make_float2(__fmul_rn(d, v.x), __fmul_rn(d, v.y));
+        }
+        out[(size_t)(s0 + j) * cstride + c] = o;
     }
     for (int j = threadIdx.x; j < ns; j += kTrThreads) {
         const float d = dsh[j];
@@ -807,6 +1045,47 @@ int launch(fr_plan p, const GridParams &P, long long nitems, long long nsplits, 
     }
     kern<<<grid, threads, smem, s>>>(P);
     FR_CHECK_LAUNCH("grid_tiles_kernel");
+    if (ev) FR_CUDA(cudaEventRecord(ev[1], s));
+    return launch_reduce<R>(P, nsplits, s);
+}
+
+template <int R>
+int launch_taps(fr_plan p, const GridParams &P, long long nitems, long long nsplits, cudaStream_t s)
+{
+    // per-item scales first (every launched item, so the indices match
+    // blockIdx.x); the bounds go to the scratch past the scales
+    {
+        const int threads = 256;
+        const long long blocks = (nitems * 32 + threads - 1) / threads;
+        const long long boff = (nitems + 1) & ~1ll;  // 8-byte aligned float2
+        float2 *bound = reinterpret_cast<float2 *>(const_cast<float *>(P.item_inv) + boff);
+        item_bound_kernel<<<(unsigned)blocks, threads, 0, s>>>(P.items, nitems, P.trecs, P.mag, bound);
+        FR_CHECK_LAUNCH("item_bound_kernel");
+        item_inv_kernel<<<(unsigned)std::min<long long>((nitems + threads - 1) / threads, 152 * 8), threads, 0, s>>>(
+            bound, nitems, P.lut_absmax, const_cast<float *>(P.item_inv));
+        FR_CHECK_LAUNCH("item_inv_kernel");
+    }
+    const TapSmem m = tap_smem_layout(P.K, R, P.L);
+    const size_t smem = m.end + 128;
+    if (smem > 227 * 1024) return fail(FR_ERR_UNSUPPORTED, "tap-list scatter does not fit in shared memory");
+    auto kern = grid_taps_kernel<R>;
+    if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)nitems, (unsigned)P.ngroups);
+    cudaEvent_t *ev = nullptr;
+    if (p->profile) {
+        if (p->prof_used * 2 + 2 > (int)p->prof_ev.size()) {
+            cudaEvent_t a, b;
+            FR_CUDA(cudaEventCreate(&a));
+            FR_CUDA(cudaEventCreate(&b));
+            p->prof_ev.push_back(a);
+            p->prof_ev.push_back(b);
+        }
+        ev = &p->prof_ev[p->prof_used * 2];
+        p->prof_used++;
+        FR_CUDA(cudaEventRecord(ev[0], s));
+    }
+    kern<<<grid, kWarps * 32, smem, s>>>(P);
+    FR_CHECK_LAUNCH("grid_taps_kernel");
     if (ev) FR_CUDA(cudaEventRecord(ev[1], s));
     return launch_reduce<R>(P, nsplits, s);
 }
@@ -882,19 +1161,30 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.skip_empty = skip_empty ? 1 : 0;
     const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
     P.mag = nullptr;
-    if (p->kspace_sample_major && channels >= 4 && p->n > 0 && trsmem <= 96 * 1024) {
-        if (p->kt.reserve(p->n * (size_t)channels * sizeof(float2)) || p->kmag.reserve(p->n * sizeof(float)))
+    P.kstride = channels;
+    if (p->err_host && *p->err_host) {  // a kernel of an earlier call found an internal error
+        const int e = *p->err_host;
+        *p->err_host = 0;
+        return fail(e, "the plan's tap lists overflowed a sample slot (internal error)");
+    }
+    // the tap-list scatter reads each record's coil values from the
+    // sample-major copy; the geometry scatter uses the copy from 4 coils on
+    const bool taps = p->tap_words > 0 && R <= 32;
+    if (p->kspace_sample_major && (channels >= 4 || taps) && p->n > 0 && trsmem <= 96 * 1024) {
+        const int cstride = channels + (channels & 1);  // even: rows start on 16-byte boundaries
+        if (p->kt.reserve(p->n * (size_t)cstride * sizeof(float2)) || p->kmag.reserve(p->n * sizeof(float)))
             return FR_ERR_OUT_OF_MEMORY;
         if (trsmem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)trsmem));
         transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
             reinterpret_cast<const float2 *>(d_kdata), d_dcf, p->kt.as<float2>(), p->kmag.as<float>(),
-            (long long)p->n, channels);
+            (long long)p->n, channels, cstride);
         FR_CHECK_LAUNCH("transpose_kspace_kernel");
         P.kdata = p->kt.as<float>();
         P.sample_major = 1;
         P.mag = p->kmag.as<float>();
+        P.kstride = cstride;
     }
     if (p->nslots > 0) {
         size_t bytes = (size_t)p->nslots * P.ngroups * (size_t)P.K * R * 4;
@@ -905,6 +1195,21 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     // zero-fill items are last in the list)
     const long long nlaunch = skip_empty ? p->nitems_occupied : p->nitems;
     if (nlaunch == 0) return FR_OK;
+    if (taps && P.sample_major) {
+        P.trecs = p->trecs.as<unsigned long long>();
+        P.taps = p->taps.as<unsigned>();
+        P.lutw = p->lut_d.as<float>();
+        P.tap_words = p->tap_words;
+        // nlaunch item scales, then (from an even word) nlaunch float2 bounds
+        const size_t words = (((size_t)nlaunch + 1) & ~(size_t)1) + 2 * (size_t)nlaunch;
+        if (p->item_inv.reserve(words * 4)) return FR_ERR_OUT_OF_MEMORY;
+        P.item_inv = p->item_inv.as<float>();
+        switch (R) {
+        case 8: return launch_taps<8>(p, P, nlaunch, p->nsplits, s);
+        case 16: return launch_taps<16>(p, P, nlaunch, p->nsplits, s);
+        case 32: return launch_taps<32>(p, P, nlaunch, p->nsplits, s);
+        }
+    }
     if (p->dim == 3) {
         switch (R) {
         case 8: return launch<3, 8>(p, P, nlaunch, p->nsplits, s);

@@ -115,6 +115,21 @@ struct fr_plan_s {
     fr::DevBuf tile_mask;     // ntiles bits: tile holds bin records (recon path skips the others)
     bool kspace_sample_major = true;  // cleared by FR_KSPACE_COIL_MAJOR=1
 
+    // Tap lists: every sample's kernel taps evaluated once per trajectory by
+    // the plan (GridLut.cpp:98-136 geometry), so the scatter reads them
+    // instead of evaluating the geometry of each of the sample's bin records.
+    // Slot of sample s: tap_words words holding the runs of its records (one
+    // per tile it touches, in the plan's tile-walk order).  Tap word:
+    // tile-local cell | LUT index << 13.
+    bool taps_enabled = true;  // cleared by FR_PLAN_NO_TAP_LISTS
+    int tap_words = 0;         // 0: this plan has no tap lists
+    int tap_layout_words = 0;  // tap_slot_layout of this plan (computed once)
+    fr::DevBuf taps;           // n x tap_words words
+    fr::DevBuf trecs;          // npairs words, in bin order: sample | first word << 32 | taps << 40
+    fr::DevBuf item_inv;       // per work item: inverse fixed-point scale, then the items' bounds
+    int *err_host = nullptr;   // mapped pinned word the kernels set on an internal error
+    int *err_dev = nullptr;
+
     // scatter-kernel timing (fr_plan_profile)
     bool profile = false;
     std::vector<cudaEvent_t> prof_ev;  // pairs (start, stop)
@@ -195,6 +210,11 @@ long long plan_scan_blocks(long long ntiles);
 // long item that the whole launch waits for), at most 4096.
 int plan_chunk(size_t n, int dim);
 int plan_stripes();  // bin-counter stripes per tile
+// Tap-list slot of a sample for a kernel half-width: words per sample, an
+// upper bound on the lattice points strictly inside a ball of radius hw.
+void tap_slot_layout(int dim, float hw, int *words);
+constexpr int kTapCellBits = 13;            // tile-local cell index bits of a tap word
+constexpr int kTapRecMax = 60;              // samples with more taps use the geometry scatter
 int plan_into(const PlanInto &pi, const float *d_traj, size_t n, cudaStream_t s, PlanIntoOut *out);
 
 // Grid from a plan held in caller-provided memory (no allocation).

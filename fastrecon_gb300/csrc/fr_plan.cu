@@ -360,6 +360,168 @@ __global__ void fill_kernel(const float4 *__restrict__ traj, size_t n, BinGeom g
     }
 }
 
+// Tap lists (the scatter's taps, evaluated once per trajectory).
+struct TapGeom {
+    unsigned *taps;                  // n x words
+    unsigned long long *trecs;       // in bin order, beside the (sample | box) records
+    const float4 *lut_e;             // {thr[k+1], lut[k], lut[k+1], 0}
+    float smax, kc;
+    int L, words;                    // tap words per sample slot
+    int *err;                        // set when a slot would overflow (never, by the slot bound)
+};
+
+// Exact LUT index of s2 = dk^2 < smax, as the scatter's weight lookup: a
+// first guess from an approximate square root (the exact index or one below)
+// and one exact threshold test (thr[k] = smallest s with index >= k).
+__device__ __forceinline__ int tap_lut_index(float s2, const float4 *__restrict__ lut_e, float kc, int L)
+{
+    float a;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(s2));
+    const int k0 = (int)fminf(fmaf(a, kc, 0.25f), (float)(L - 1));
+    return k0 + (s2 >= __ldg(&lut_e[k0].x) ? 1 : 0);
+}
+
+// Pass 3 with tap lists: the records of fill_kernel, and for each record the
+// taps of the sample inside the record's tile, evaluated with the
+// reference's geometry (GridLut.cpp:98-136: the clamped cell range, dk^2 =
+// (dz^2 + dy^2) + dx^2 unfused, valid iff dk < kHW), as tap words in the
+// sample's slot: one run per record, in the order of the sample's tile
+// walk; trecs[pos] gives the run (first word, count).  Each thread walks its
+// sample's whole cell range twice (the same box shape for neighbouring
+// samples, so the lanes of a warp stay together): once to count the taps
+// per record, once to place them, into a shared-memory copy of the slot;
+// the block's slots, consecutive in memory, are then written out with
+// coalesced 16-byte stores.
+constexpr int kFillThreads = 256;
+constexpr int kFillRecMax = 32;  // records per sample (tiles a sample's range touches) the fill supports
+
+// cnt[j * kFillThreads], off[j * kFillThreads]: this thread's tap count and
+// first slot word of record j (record-major, so a warp's lanes touch
+// consecutive bytes).
+__device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg, const float *c, const int *s,
+                                            const int *e, const TileWalk &w, bool place, unsigned char *cnt,
+                                            const unsigned char *off, unsigned *slot)
+{
+    float fz = (float)s[2];
+    for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
+        const float dz = g.dim == 3 ? __fsub_rn(fz, c[2]) : 0.f;
+        const float dz2 = __fmul_rn(dz, dz);
+        const int jz = tile_div(g, z, 2) - w.lo[2];
+        const int lz = z - (w.lo[2] + jz) * g.tile[2];
+        float fy = (float)s[1];
+        for (int y = s[1]; y <= e[1]; ++y, fy = __fadd_rn(fy, 1.f)) {
+            const float dy = __fsub_rn(fy, c[1]);
+            const float dzy = __fadd_rn(dz2, __fmul_rn(dy, dy));
+            const int jy = tile_div(g, y, 1) - w.lo[1];
+            const int ly = y - (w.lo[1] + jy) * g.tile[1];
+            const int jzy = (jz * w.n[1] + jy) * w.n[0];
+            const int rowzy = (lz * g.tile[1] + ly) * g.tile[0];
+            float fx = (float)s[0];
+            for (int x = s[0]; x <= e[0]; ++x, fx = __fadd_rn(fx, 1.f)) {
+                const float dx = __fsub_rn(fx, c[0]);
+                const float s2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
+                if (s2 < tg.smax) {
+                    const int jx = tile_div(g, x, 0) - w.lo[0];
+                    const int j = (jzy + jx) * kFillThreads;
+                    const int k = cnt[j]++;
+                    if (place) {
+                        const int wi = off[j] + k;
+                        const int lx = x - (w.lo[0] + jx) * g.tile[0];
+                        if (wi < tg.words)
+                            slot[wi] = (unsigned)(rowzy + lx) |
+                                       ((unsigned)tap_lut_index(s2, tg.lut_e, tg.kc, tg.L) << kTapCellBits);
+                    }
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *__restrict__ traj, size_t n,
+                                                                 BinGeom g, TapGeom tg,
+                                                                 const long long *__restrict__ stripe_base,
+                                                                 int *__restrict__ tile_fill,
+                                                                 unsigned long long *__restrict__ recs)
+{
+    // [kFillThreads][S] slot words (S = words | 1: odd, no bank conflicts),
+    // then the tap counts and the run offsets, kFillRecMax x kFillThreads each
+    extern __shared__ unsigned stage[];
+    const int S = tg.words | 1;
+    const int lane = threadIdx.x & 31;
+    unsigned *mine = stage + threadIdx.x * S;
+    unsigned char *cnt = reinterpret_cast<unsigned char *>(stage + kFillThreads * S) + threadIdx.x;
+    unsigned char *off = cnt + kFillRecMax * kFillThreads;
+    for (size_t base = blockIdx.x * (size_t)kFillThreads; base < n; base += (size_t)gridDim.x * kFillThreads) {
+        size_t i = base + threadIdx.x;
+        TileWalk w;
+        int s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+        float c[3] = {0.f, 0.f, 0.f};
+        int cnt_t = 0;
+        if (i < n) {
+            float4 q = traj[i];
+            cnt_t = sample_tiles(g, q, w, s, e);
+            c[0] = q.x;
+            c[1] = q.y;
+            c[2] = q.z;
+        } else {
+            w.lo[0] = w.lo[1] = w.lo[2] = 0;
+            w.n[0] = w.n[1] = w.n[2] = 1;
+        }
+        // taps per record, then each record's first word, then the taps
+        for (int j = 0; j < cnt_t; ++j) cnt[j * kFillThreads] = 0;
+        if (cnt_t > 0) sample_taps(g, tg, c, s, e, w, false, cnt, off, mine);
+        int tot = 0;
+        for (int j = 0; j < cnt_t; ++j) {
+            off[j * kFillThreads] = (unsigned char)min(tot, 255);
+            tot += cnt[j * kFillThreads];
+            cnt[j * kFillThreads] = 0;
+        }
+        if (tot > tg.words) *tg.err = FR_ERR_CAPACITY;  // never: the slot bounds every sample's taps
+        if (cnt_t > 0) sample_taps(g, tg, c, s, e, w, true, cnt, off, mine);
+
+        const int stripe = stripe_of(base + threadIdx.x - lane);
+        int maxcnt = __reduce_max_sync(0xffffffffu, cnt_t);
+        for (int j = 0; j < maxcnt; ++j, w.next()) {
+            bool valid = j < cnt_t;
+            int t = valid ? w.tile(g) : -1 - lane;
+            int run, head_lane;
+            lane_runs(t, lane, run, head_lane);
+            int basepos = 0;
+            const int ts = t * kStripes + stripe;
+            if (valid && lane == head_lane) basepos = atomicAdd(&tile_fill[ts], run);
+            basepos = __shfl_sync(0xffffffffu, basepos, head_lane);
+            if (valid) {
+                long long pos = stripe_base[ts] + basepos + (lane - head_lane);
+                unsigned box = tile_box(g, c, s, e, w.lo[0] + w.jx, w.lo[1] + w.jy, w.lo[2] + w.jz);
+                recs[pos] = ((unsigned long long)box << 32) | (unsigned long long)i;
+                const int ntap = tot > tg.words ? 0 : cnt[j * kFillThreads];  // a dropped run (never) has no taps
+                tg.trecs[pos] = (unsigned long long)i | ((unsigned long long)off[j * kFillThreads] << 32) |
+                                ((unsigned long long)ntap << 40);
+            }
+        }
+        __syncthreads();
+        // the block's slots are words [base * words, (base + nv) * words):
+        // 16-byte aligned (base is a multiple of kFillThreads), copied as uint4
+        const int nv = (int)min((size_t)kFillThreads, n - base);
+        const int total = nv * tg.words;
+        uint4 *dst = reinterpret_cast<uint4 *>(tg.taps + base * (size_t)tg.words);
+        for (int qd = threadIdx.x; qd < total / 4; qd += kFillThreads) {
+            unsigned v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int wi = 4 * qd + k, smp = wi / tg.words;
+                v[k] = stage[smp * S + (wi - smp * tg.words)];
+            }
+            dst[qd] = make_uint4(v[0], v[1], v[2], v[3]);
+        }
+        for (int wi = (total & ~3) + threadIdx.x; wi < total; wi += kFillThreads) {
+            const int smp = wi / tg.words;
+            tg.taps[base * (size_t)tg.words + wi] = stage[smp * S + (wi - smp * tg.words)];
+        }
+        __syncthreads();
+    }
+}
+
 __device__ __forceinline__ TileScan tile_value(int cnt, int chunk)
 {
     TileScan v;
@@ -642,7 +804,37 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         p->items.reserve(std::max<long long>(p->nitems, 1) * sizeof(WorkItem)) ||
         p->splits.reserve(std::max<long long>(tot.splits, 1) * sizeof(SplitTile)))
         return FR_ERR_OUT_OF_MEMORY;
-    if (n > 0) {
+    // tap lists, when the tile and kernel allow them and the memory is there
+    p->tap_words = 0;
+    if (p->taps_enabled && n > 0 && p->err_dev && p->L < (1 << (32 - kTapCellBits)) &&
+        (long long)p->tile[0] * p->tile[1] * p->tile[2] <= (1 << kTapCellBits)) {
+        if (p->tap_layout_words == 0) tap_slot_layout(p->dim, p->hw, &p->tap_layout_words);
+        const int words = p->tap_layout_words;
+        // tiles one sample's cell range (at most floor(2 hw) + 1 cells per axis) can touch
+        const int F = (int)std::floor(2.0 * p->hw) + 1;
+        int recmax = 1;
+        for (int d = 0; d < p->dim; ++d) recmax *= (F - 1 + p->tile[d] - 1) / p->tile[d] + 1;
+        if (words <= kTapRecMax && recmax <= kFillRecMax && !p->taps.reserve(n * (size_t)words * 4) &&
+            !p->trecs.reserve(std::max<long long>(tot.pairs, 1) * 8))
+            p->tap_words = words;
+    }
+    if (n > 0 && p->tap_words > 0) {
+        TapGeom tg;
+        tg.taps = p->taps.as<unsigned>();
+        tg.trecs = p->trecs.as<unsigned long long>();
+        tg.lut_e = p->lut_e.as<float4>();
+        tg.smax = p->lut_smax;
+        tg.kc = p->lut_kc;
+        tg.L = p->L;
+        tg.words = p->tap_words;
+        tg.err = p->err_dev;
+        const size_t smem = (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * kFillRecMax);
+        if (smem > 48 * 1024)
+            FR_CUDA(cudaFuncSetAttribute(fill_taps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        fill_taps_kernel<<<grid_blocks(n, kFillThreads), kFillThreads, smem, s>>>(
+            traj, n, g, tg, p->stripe_base.as<long long>(), p->tile_fill.as<int>(), p->pairs.as<unsigned long long>());
+        FR_CHECK_LAUNCH("fill_taps_kernel");
+    } else if (n > 0) {
         fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, p->stripe_base.as<long long>(), p->tile_fill.as<int>(),
                                                         p->pairs.as<unsigned long long>());
         FR_CHECK_LAUNCH("fill_kernel");
@@ -713,6 +905,32 @@ int normalize_run(const float *d_traj, size_t n, int dim, unsigned G, float *d_o
 }
 
 int plan_stripes() { return kStripes; }
+
+void tap_slot_layout(int dim, float hw, int *words)
+{
+    // Most lattice points strictly inside a ball of radius hw, over all
+    // centres: centres on a grid of step h over the unit cell, counted with
+    // radius hw + h sqrt(d) / 2 (every centre lies that close to a grid
+    // centre), so the count bounds every sample's taps from above.
+    const double h = 1.0 / 16, r = (double)hw + h * std::sqrt((double)dim) / 2, r2 = r * r;
+    const int R = (int)std::ceil(r) + 1;
+    int nmax = 0;
+    const int nc = 16, ncz = dim == 3 ? 16 : 1;
+    for (int cz = 0; cz < ncz; ++cz)
+        for (int cy = 0; cy < nc; ++cy)
+            for (int cx = 0; cx < nc; ++cx) {
+                const double c[3] = {cx * h, cy * h, cz * h};
+                int cnt = 0;
+                for (int z = (dim == 3 ? -R : 0); z <= (dim == 3 ? R + 1 : 0); ++z)
+                    for (int y = -R; y <= R + 1; ++y)
+                        for (int x = -R; x <= R + 1; ++x) {
+                            const double dx = x - c[0], dy = y - c[1], dz = dim == 3 ? z - c[2] : 0.0;
+                            if (dx * dx + dy * dy + dz * dz < r2) ++cnt;
+                        }
+                nmax = std::max(nmax, cnt);
+            }
+    *words = nmax;
+}
 
 int plan_chunk(size_t n, int dim)
 {

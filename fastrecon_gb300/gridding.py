@@ -59,7 +59,7 @@ class GridPlan:
 
     def __init__(self, dim: int, grid_size: int, kernel_width: float = 4.0, lut=None, lut_length: int = 512,
                  overgrid_factor: float = 2.0, tile=(0, 0, 0), coil_group: int = 0, chunk: int = 0,
-                 checkerboard: bool = False):
+                 checkerboard: bool = False, tap_lists: bool = True):
         self.lib = capi.load()
         if lut is None:
             lut = kb_lut(kernel_width, overgrid_factor, lut_length)
@@ -74,7 +74,7 @@ class GridPlan:
             d.tile[i] = int(tile[i]) if i < len(tile) else 0
         d.coil_group = coil_group
         d.chunk = chunk
-        d.flags = capi.FR_PLAN_CHECKERBOARD if checkerboard else 0
+        d.flags = (capi.FR_PLAN_CHECKERBOARD if checkerboard else 0) | (0 if tap_lists else capi.FR_PLAN_NO_TAP_LISTS)
         h = C.c_void_p()
         check(self.lib.fr_plan_create(C.byref(d), C.byref(h)), "fr_plan_create")
         self.h = h
@@ -122,6 +122,12 @@ class GridPlan:
         v = [C.c_longlong() for _ in range(4)]
         check(self.lib.fr_plan_stats(self.h, *[C.byref(x) for x in v]), "fr_plan_stats")
         return dict(tiles=v[0].value, pairs=v[1].value, items=v[2].value, slots=v[3].value)
+
+    def tap_words(self) -> int:
+        """4-byte words per sample of the plan's tap lists (0: none)."""
+        q = C.c_int()
+        check(self.lib.fr_plan_tap_words(self.h, C.byref(q)), "fr_plan_tap_words")
+        return q.value
 
     def bins(self, stream=None):
         torch = _torch()

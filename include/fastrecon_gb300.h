@@ -82,11 +82,15 @@ enum {
     FR_PLAN_CHECKERBOARD = 1u << 0, /* multiply grid cell (x,y,z) by (-1)^(x+y+z)
                                        on output, which makes the backward FFT
                                        produce the fftShift-ed image (even G) */
-    FR_PLAN_PRENORMALIZED = 1u << 1 /* the trajectory given to
+    FR_PLAN_PRENORMALIZED = 1u << 1, /* the trajectory given to
                                        fr_plan_set_trajectory is already in
                                        grid units (ReconData::normalizeTraj was
                                        applied, e.g. by fr_normalize_trajectory):
                                        bin it as is */
+    FR_PLAN_NO_TAP_LISTS = 1u << 2  /* keep no per-sample tap lists: the
+                                       scatter evaluates each bin record's
+                                       kernel taps itself (saves ~170 bytes
+                                       per 3D sample of device memory, slower) */
 };
 
 /* ReconData::normalizeTraj (ReconData.cpp:211-225) on the device: component
@@ -137,6 +141,14 @@ int fr_plan_sample_ranges(fr_plan plan, int *d_start, int *d_end, void *stream);
  * split-tile partial slots.  Host ints. */
 int fr_plan_stats(fr_plan plan, long long *tiles, long long *pairs, long long *items,
                   long long *partial_slots);
+
+/* Tap lists of the current trajectory: 4-byte words per sample of the
+ * plan's per-sample tap slots, or 0 when the plan keeps none (the scatter
+ * then evaluates the taps of each bin record itself).  The plan evaluates
+ * every sample's kernel taps once per trajectory (GridLut.cpp:120-136
+ * geometry) -- the counterpart of cuGridLut::plan materialising (cell,
+ * sample) pairs (cuGridLut.cu:50-113) -- in one word per tap. */
+int fr_plan_tap_words(fr_plan plan, int *words_per_sample);
 
 /* Sorted bin lists (device): tile_offset[tiles+1] (int64) and
  * pairs[pairs] (uint32 sample index), for bit-exact binning checks. */
