@@ -13,8 +13,9 @@ explicit L2 flush is needed between steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference's CPU algorithm (the CPU oracle, a
-C restatement of GridLut/ImageFilter, OpenMP) on this host's cores on a
-bounded sample of the same workload and extrapolates a full step.
+C restatement of GridLut/ImageFilter, with the reference's OpenMP threading)
+on this host's cores: every timed step is one complete recon of the same
+workload, measured (about 15 s per kooshball step on 16 cores).
 """
 from __future__ import annotations
 
@@ -152,90 +153,169 @@ def algorithmic_bytes(w):
 
 
 # --------------------------------------------------------------------------
-# CPU baseline: the oracle (reference algorithm) on a bounded sample
+# The reference's CPU path (the oracle, a C restatement of the reference's
+# algorithm), timed on this host's cores: the reference arm and cpu_baseline
 # --------------------------------------------------------------------------
 
-def cpu_step(w, traj, dcf, kd, threads_grid, threads_fft, spoke_frac, fft_coils):
-    """One bounded CPU recon step; returns (extrapolated full-step seconds,
-    description)."""
-    import numpy as np
-
-    from oracle.pyoracle import Oracle
-    o = Oracle()
-    R = w["readout"]
-    S = max(1, int(w["spokes"] * spoke_frac))
-    n = S * R
-    N = w["spokes"] * R
-    C = w["coils"]
-    dim = w["dim"]
-    G = int(np.float32(w["recon"]) * np.float32(w["os"]))
-    lut = o.kb_lut(w["width"], w["os"], w["lut"])
-    t0 = time.perf_counter()
-    tn, *_ = o.normalize_traj(traj[:n], dim, G)
-    grid = o.grid(tn, dcf[:n], kd[:, :n], dim, G, w["width"], lut, threads=threads_grid)
-    t1 = time.perf_counter()
-    sub = o.fft(grid[:fft_coils], dim, G, +1, threads_fft)
-    for c in range(fft_coils):
-        sub[c] = o.fft_shift(sub[c], dim, G)
-    t2 = time.perf_counter()
-    rec = (w["recon"], w["recon"], w["recon"] if dim == 3 else 1)
-    o.sos(grid, dim, G, rec)
-    t3 = time.perf_counter()
-    full = (t1 - t0) * (N / n) + (t2 - t1) * (C / fft_coils) + (t3 - t2)
-    desc = (f"{S} of {w['spokes']} spokes x {R} samples x {C} coils gridded ({threads_grid} threads, OpenMP over "
-            f"coils as GridLut::execute), backward FFT + fftShift of {fft_coils} of {C} coils (oracle mixed-radix "
-            f"FFT, stand-in for FFTW3f, {threads_fft} threads), SoS of all coils; full step extrapolated linearly "
-            f"(grid x {N / n:.1f}, FFT x {C / fft_coils:.1f})")
-    return full, desc, (t3 - t0)
-
-
-def cpu_sample_inputs(w, kd_full=None):
-    import numpy as np
-
+def ref_inputs(w):
+    """The workload's raw trajectory, DCF and k-space as host arrays, from the
+    same seeded generator as the measured arm.  The k-space is synthesised on
+    the GPU when one is present (input synthesis only: nothing of the timed
+    region runs there) and copied to host memory."""
     from fastrecon_gb300 import synth
     traj = synth.radial_2d(w["spokes"], w["readout"]) if w["dim"] == 2 else \
         synth.kooshball_3d(w["spokes"], w["readout"])
     dcf = synth.ramp_dcf(traj, w["dim"], w["dcf_power"])
-    return traj, dcf
+    try:
+        import torch
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    if gpu:
+        kd = synth.kspace(traj, w["dim"], w["recon"], w["coils"], seed=0, xp=torch, device="cuda").cpu().numpy()
+        torch.cuda.empty_cache()
+    else:
+        kd = synth.kspace(traj, w["dim"], w["recon"], w["coils"], seed=0)
+    return traj, dcf, kd
 
 
-def cpu_fractions(w):
-    if w["dim"] == 3:
-        return 1.0 / 8, 2
-    return 1.0, w["coils"]
+class RefRecon:
+    """One reconstruction as Program/Main.cpp:101-181 runs it, with the
+    reference's threading, on the CPU oracle:
+    * ReconData::normalizeTraj, one thread (ReconData.cpp:201-225);
+    * GridLut::execute: OpenMP over coils, threads = min(coils, cores)
+      (GridLut.cpp:53-78, Main.cpp:111);
+    * ImageFilter::fftExecute: one single-threaded backward FFT per coil,
+      coils spread over the host threads (FFT.cpp:56-90).  FFTW3f is absent
+      on these hosts: scipy.fft (pocketfft, single precision, unnormalised
+      backward transform) stands in for it;
+    * ImageFilter::fftShift: the reference's swap loops per coil, coils over
+      the threads (ImageFilter.cpp:40-53);
+    * ImageFilter::SOS, one thread (ImageFilter.cpp:159-209), then |.|."""
+
+    def __init__(self, w, traj, dcf, kd):
+        import numpy as np
+
+        from oracle.pyoracle import Oracle
+        self.o = Oracle()
+        self.w, self.traj, self.dcf, self.kd = w, traj, dcf, np.ascontiguousarray(kd, np.complex64)
+        self.dim = w["dim"]
+        self.G = int(np.float32(w["recon"]) * np.float32(w["os"]))
+        self.lut = self.o.kb_lut(w["width"], w["os"], w["lut"])
+        self.ncpu = os.cpu_count() or 1
+        self.tg = min(w["coils"], self.ncpu)
+        self.rec = (w["recon"], w["recon"], w["recon"] if self.dim == 3 else 1)
+        try:
+            import scipy.fft as sfft
+            self.sfft = sfft
+            self.fft_desc = "scipy.fft (pocketfft, complex64, one thread per coil) standing in for FFTW3f"
+        except ImportError:
+            self.sfft = None
+            self.fft_desc = "the oracle's FP64 mixed-radix FFT standing in for FFTW3f"
+
+    def _fft_one(self, g):
+        if self.sfft is None:
+            g[:] = self.o.fft(g[None], self.dim, self.G, +1, 1)[0]
+            return
+        shp = (self.G,) * self.dim
+        g.reshape(shp)[...] = self.sfft.ifftn(g.reshape(shp), norm="forward", workers=1)
+
+    def step(self, n=None, fft_coils=None):
+        """One recon (of the first n samples and fft_coils coils when given:
+        warm-up only); returns seconds per stage."""
+        from concurrent.futures import ThreadPoolExecutor
+        w, o, dim, G = self.w, self.o, self.dim, self.G
+        n = n or self.traj.shape[0]
+        t0 = time.perf_counter()
+        tn, *_ = o.normalize_traj(self.traj[:n], dim, G)
+        grid = o.grid(tn, self.dcf[:n], self.kd[:, :n], dim, G, w["width"], self.lut, threads=self.tg)
+        t1 = time.perf_counter()
+        cs = range(fft_coils if fft_coils is not None else grid.shape[0])
+        with ThreadPoolExecutor(self.ncpu) as ex:
+            list(ex.map(lambda c: self._fft_one(grid[c]), cs))
+            t2 = time.perf_counter()
+            list(ex.map(lambda c: o.fft_shift_inplace(grid[c], dim, G), cs))
+        t3 = time.perf_counter()
+        img = abs(o.sos(grid, dim, G, self.rec).real)
+        t4 = time.perf_counter()
+        del grid, img
+        return {"grid": t1 - t0, "fft": t2 - t1, "shift": t3 - t2, "sos": t4 - t3, "total": t4 - t0}
+
+    def describe(self, warm):
+        w = self.w
+        return (f"complete recon per step: all {w['spokes']} spokes x {w['readout']} samples x {w['coils']} coils "
+                f"gridded ({self.tg} threads, OpenMP over coils as GridLut::execute), backward FFT of every coil "
+                f"({self.fft_desc}; coils over {self.ncpu} threads as FFT.cpp), fftShift per coil, SOS; measured, "
+                f"not extrapolated{warm}")
+
+
+def fp64_errors(w, traj, dcf, kd, torch):
+    """GPU grid (fr_grid, default tiling and work items) vs the oracle's FP64
+    gridding and its FP32 restatement of the reference, on the first 2 coils
+    of the workload and on the whole 2D radial configuration."""
+    import numpy as np
+
+    import fastrecon_gb300 as fr
+    from oracle.pyoracle import Oracle
+    o = Oracle()
+
+    def rel(a, b):
+        a = np.asarray(a).astype(np.complex128).ravel()
+        b = np.asarray(b).astype(np.complex128).ravel()
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    out = {}
+    cases = [(w, traj, dcf, kd[:2], f"{w['desc'].split(':')[0]}, 2 of {w['coils']} coils")]
+    if w is not WORKLOADS["radial2d"]:
+        r2 = WORKLOADS["radial2d"]
+        t2, d2, k2, _ = make_inputs(r2, torch, traj.device)
+        cases.append((r2, t2, d2, k2, "2D radial 256 x 512, 8 coils"))
+    for wk, t, d, k, name in cases:
+        G = fr.grid_size(wk["recon"], wk["os"])
+        lut = o.kb_lut(wk["width"], wk["os"], wk["lut"])
+        plan = fr.GridPlan(wk["dim"], G, wk["width"], lut=lut)
+        plan.set_trajectory(t)
+        g = plan.grid(k.contiguous(), d).cpu().numpy()
+        del plan
+        tn, *_ = o.normalize_traj(t.cpu().numpy(), wk["dim"], G)
+        kn = k.cpu().numpy()
+        g64 = o.grid_f64_bands(tn, d.cpu().numpy(), kn, wk["dim"], G, wk["width"], lut)
+        ref = o.grid_bands(tn, d.cpu().numpy(), kn, wk["dim"], G, wk["width"], lut)
+        out[name] = {"gpu_vs_fp64": rel(g, g64), "gpu_vs_reference_fp32": rel(g, ref),
+                     "reference_fp32_vs_fp64": rel(ref, g64)}
+        del g, g64, ref
+    return out
 
 
 def run_reference(args, w):
-    import numpy as np
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    ncpu = os.cpu_count() or 1
-    frac, fft_coils = cpu_fractions(w)
-    traj, dcf = cpu_sample_inputs(w)
-    n = int(w["spokes"] * frac) * w["readout"]
-    from fastrecon_gb300 import synth
-    kd = synth.kspace(traj[:n], w["dim"], w["recon"], w["coils"], seed=0)
-    tg = min(w["coils"], ncpu)
+    traj, dcf, kd = ref_inputs(w)
+    r = RefRecon(w, traj, dcf, kd)
+    # warm-up steps (untimed): a small slice of the gridding and one coil's
+    # transform, enough to page in the code and start the thread pools
+    n_warm = max(w["readout"], (w["spokes"] // 64) * w["readout"])
     for _ in range(args.warmup):
-        cpu_step(w, traj, dcf, kd, tg, ncpu, frac, fft_coils)
-    fulls, desc, wall = [], "", 0.0
+        r.step(n=n_warm, fft_coils=1)
+    stages = []
     for _ in range(args.steps):
-        f, desc, wl = cpu_step(w, traj, dcf, kd, tg, ncpu, frac, fft_coils)
-        fulls.append(f)
-        wall += wl
-    t = statistics.mean(fulls)
+        stages.append(r.step())
+    t = statistics.mean(s["total"] for s in stages)
     N = w["spokes"] * w["readout"]
     value = N * w["coils"] / t / 1e6
+    stage_ms = {k: 1e3 * statistics.mean(s[k] for s in stages) for k in stages[0]}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["desc"], "samples_per_coil": N, "coils": w["coils"]},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": max(tg, ncpu), "kind": "port",
-                             "sample": desc},
+            "stage_ms": stage_ms,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": r.ncpu, "kind": "port",
+                             "sample": r.describe("; warm-up steps: 1/64 of the spokes and one coil's FFT")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "reference CPU algorithm (oracle port of GridLut/ImageFilter; the reference's own sources "
-                    "need Qt/GSL/FFTW and x86-only builds are not carried to this host)"}
+            "note": "reference CPU algorithm (the oracle's C restatement of GridLut/ImageFilter, pinned bit for bit "
+                    "to the reference's own CPU sources where they build; those need Qt/GSL/FFTW and are not "
+                    "carried to this host)"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -400,14 +480,20 @@ def run_ours(args, w):
         "e2e": e2e,
     }
     if not args.no_cpu_baseline and ws == 1:
-        frac, fft_coils = cpu_fractions(w)
-        ncpu = os.cpu_count() or 1
-        ctraj, cdcf = cpu_sample_inputs(w)
-        n = int(w["spokes"] * frac) * w["readout"]
-        ckd = kd[:, :n].cpu().numpy()
-        full, desc, _ = cpu_step(w, ctraj, cdcf, ckd, min(C, ncpu), ncpu, frac, fft_coils)
-        line["cpu_baseline"] = {"value": N * C / full / 1e6, "unit": UNIT, "cores": ncpu, "kind": "port",
-                                "sample": desc, "ms_per_step": full * 1e3}
+        # one complete recon of the same workload by the reference's CPU
+        # algorithm on this host (a bounded sample of the CPU work: ~15 s)
+        r = RefRecon(w, traj.cpu().numpy(), dcf.cpu().numpy(), kd.cpu().numpy())
+        r.step(n=max(w["readout"], (w["spokes"] // 64) * w["readout"]), fft_coils=1)
+        st = r.step()
+        line["cpu_baseline"] = {"value": N * C / st["total"] / 1e6, "unit": UNIT, "cores": r.ncpu, "kind": "port",
+                                "sample": r.describe(" (one step, after a small warm-up)"),
+                                "ms_per_step": st["total"] * 1e3,
+                                "stage_ms": {k: v * 1e3 for k, v in st.items()}}
+        del r
+        # the oracle as checker: relative L2 error of the GPU grid against
+        # the FP64 gridding oracle and against the reference's FP32
+        # algorithm, for this workload (2 of its coils) and the 2D radial
+        line["fp64_rel_l2"] = fp64_errors(w, traj, dcf, kd, torch)
     if not args.no_extras and ws == 1:
         import bench_extras
         del rec, traj, dcf, kd

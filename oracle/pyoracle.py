@@ -193,6 +193,12 @@ class Oracle:
         self.lib.orc_fft_shift(a.view(np.float32).ravel(), dim, size)
         return a
 
+    def fft_shift_inplace(self, img: np.ndarray, dim: int, G: int) -> None:
+        """``fft_shift`` on a contiguous complex64 array, in place."""
+        assert img.dtype == np.complex64 and img.flags.c_contiguous
+        size = np.array([G, G, G if dim == 3 else 1], np.uint32)
+        self.lib.orc_fft_shift(img.reshape(-1).view(np.float32), dim, size)
+
     def sos(self, imgs: np.ndarray, dim: int, G: int, recon) -> np.ndarray:
         a = np.ascontiguousarray(imgs, np.complex64)
         size = np.array([G, G, G if dim == 3 else 1], np.uint32)
