@@ -6,10 +6,12 @@
 // Layout (FR_MLP_PARAMS values): W1[64][5] | b1[64] | W2[64][64] | b2[64] |
 // W3[64] | b3.
 //
-//  * mlp_forward_kernel: one thread per sample, the BF16 parameters widened
-//    into shared memory once per CTA; first-layer units are produced one at
-//    a time and scattered into the 64 second-layer accumulators held in
-//    registers.
+//  * mlp_forward_mma_kernel (inference): the hidden layer on the tensor
+//    cores (mma.sync, BF16 operands in three terms, FP32 accumulation).
+//  * mlp_forward_kernel (FR_MLP_SIMT=1): one thread per sample, the BF16
+//    parameters widened into shared memory once per CTA; first-layer units
+//    are produced one at a time and scattered into the 64 second-layer
+//    accumulators held in registers.
 //  * backward: mlp_train_kernel does the forward pass and the per-sample
 //    reverse pass (dL/dy, the two hidden-layer deltas) and writes the
 //    per-sample activations and deltas; mlp_grad_kernel reduces the
@@ -21,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "fr_internal.h"
 
@@ -124,6 +127,134 @@ __global__ void __launch_bounds__(kFwdThreads) mlp_forward_kernel(const __nv_bfl
         float out = forward_sample(ps, xs, h2);
         if (residual) out = __fsub_rn(out, xs[1]);  // the network predicts log-DCF + log density (radius 2)
         y[s] = exp_out ? __fmul_rn(scale, expf(out)) : out;
+    }
+}
+
+// The forward pass with the hidden layer (64 x 64) on the tensor cores:
+// mma.sync m16n8k16, BF16 operands, FP32 accumulation.  One warp holds a
+// tile of 16 samples: each lane evaluates, in FP32 as forward_sample does,
+// exactly the first-layer activations its A fragments hold (2 samples x 16
+// units), splits each into three BF16 terms hi + mid + lo (the residual of
+// a BF16 rounding, twice: together within ~2^-24 of the FP32 value), and the
+// warp accumulates W2 h1 = W2 hi + W2 mid + W2 lo into FP32 fragments that
+// start from b2; the weights are BF16 already, so every product is exact
+// and the sums carry FP32 rounding only.  The output layer reduces each
+// lane's 16 units and the 4 lanes of a row with shuffles.
+__device__ __forceinline__ unsigned pack_bf16(float lo_half, float hi_half)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo_half, hi_half);
+    return *reinterpret_cast<const unsigned *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float *d, const unsigned *a, unsigned b0, unsigned b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kMmaThreads = 128;  // 4 warps, 16 samples each per step
+
+__global__ void __launch_bounds__(kMmaThreads) mlp_forward_mma_kernel(const __nv_bfloat16 *__restrict__ pb,
+                                                                      const float *__restrict__ x, long long n,
+                                                                      int exp_out, int residual, float scale,
+                                                                      float *__restrict__ y)
+{
+    __shared__ __align__(16) __nv_bfloat16 pw[NP + 7];
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) pw[p] = pb[p];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2, tig = lane & 3;
+    const unsigned *w2 = reinterpret_cast<const unsigned *>(pw + OFF_W2);  // bf16 pairs of W2[j][i], i fastest
+    const long long ntile = (n + 15) / 16;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long tile = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); tile < ntile;
+         tile += warps) {
+        const long long s0 = tile * 16 + g, s1 = s0 + 8;
+        float x0[NI], x1[NI];
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            x0[k] = s0 < n ? x[s0 * NI + k] : 0.f;
+            x1[k] = s1 < n ? x[s1 * NI + k] : 0.f;
+        }
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int j = 8 * nt + 2 * tig;
+            acc[nt][0] = acc[nt][2] = __bfloat162float(pw[OFF_B2 + j]);
+            acc[nt][1] = acc[nt][3] = __bfloat162float(pw[OFF_B2 + j + 1]);
+        }
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            // this lane's first-layer units: i0 + {0, 1} and i0 + 8 + {0, 1}
+            const int i0 = 16 * ks + 2 * tig;
+            float h[2][4];  // [sample row g / g + 8][unit i0, i0 + 1, i0 + 8, i0 + 9]
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + (u & 1) + (u >> 1) * 8;
+                float a0 = __bfloat162float(pw[OFF_B1 + i]), a1 = a0;
+#pragma unroll
+                for (int k = 0; k < NI; ++k) {
+                    const float wk = __bfloat162float(pw[OFF_W1 + i * NI + k]);
+                    a0 = fmaf(wk, x0[k], a0);
+                    a1 = fmaf(wk, x1[k], a1);
+                }
+                h[0][u] = tanhf(a0);
+                h[1][u] = tanhf(a1);
+            }
+            // three BF16 terms per activation; A registers: a0a1 row g k lo,
+            // a2a3 row g+8 k lo, a4a5 row g k hi, a6a7 row g+8 k hi
+            unsigned A[3][4];
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+#pragma unroll
+                for (int qq = 0; qq < 2; ++qq) {
+                    const float v0 = h[r][2 * qq], v1 = h[r][2 * qq + 1];
+                    const float hi0 = __bfloat162float(__float2bfloat16_rn(v0));
+                    const float hi1 = __bfloat162float(__float2bfloat16_rn(v1));
+                    const float r0 = __fsub_rn(v0, hi0), r1 = __fsub_rn(v1, hi1);
+                    const float md0 = __bfloat162float(__float2bfloat16_rn(r0));
+                    const float md1 = __bfloat162float(__float2bfloat16_rn(r1));
+                    const int reg = r + 2 * qq;
+                    A[0][reg] = pack_bf16(hi0, hi1);
+                    A[1][reg] = pack_bf16(md0, md1);
+                    A[2][reg] = pack_bf16(__fsub_rn(r0, md0), __fsub_rn(r1, md1));
+                }
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int j = 8 * nt + g;  // B column = output unit
+                const unsigned b0 = w2[(j * NH + i0) >> 1], b1 = w2[(j * NH + i0 + 8) >> 1];
+                mma_bf16_16816(acc[nt], A[2], b0, b1);
+                mma_bf16_16816(acc[nt], A[1], b0, b1);
+                mma_bf16_16816(acc[nt], A[0], b0, b1);
+            }
+        }
+        float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int j = 8 * nt + 2 * tig;
+            const float w3a = __bfloat162float(pw[OFF_W3 + j]), w3b = __bfloat162float(pw[OFF_W3 + j + 1]);
+            o0 = fmaf(w3a, tanhf(acc[nt][0]), o0);
+            o0 = fmaf(w3b, tanhf(acc[nt][1]), o0);
+            o1 = fmaf(w3a, tanhf(acc[nt][2]), o1);
+            o1 = fmaf(w3b, tanhf(acc[nt][3]), o1);
+        }
+        o0 += __shfl_xor_sync(0xffffffffu, o0, 1);
+        o0 += __shfl_xor_sync(0xffffffffu, o0, 2);
+        o1 += __shfl_xor_sync(0xffffffffu, o1, 1);
+        o1 += __shfl_xor_sync(0xffffffffu, o1, 2);
+        if (tig == 0) {
+            const float b3 = __bfloat162float(pw[OFF_B3]);
+            float out0 = __fadd_rn(o0, b3), out1 = __fadd_rn(o1, b3);
+            if (residual) {  // the network predicts log-DCF + log density (radius 2)
+                out0 = __fsub_rn(out0, x0[1]);
+                out1 = __fsub_rn(out1, x1[1]);
+            }
+            if (s0 < n) y[s0] = exp_out ? __fmul_rn(scale, expf(out0)) : out0;
+            if (s1 < n) y[s1] = exp_out ? __fmul_rn(scale, expf(out1)) : out1;
+        }
     }
 }
 
@@ -302,6 +433,13 @@ int sm_count_mlp()
     return n;
 }
 
+// FR_MLP_SIMT=1: the forward pass on the FP32 CUDA cores (A/B measurements).
+bool mlp_use_simt()
+{
+    const char *e = std::getenv("FR_MLP_SIMT");
+    return e && std::atoi(e) != 0;
+}
+
 int train_blocks(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + kFwdThreads - 1) / kFwdThreads, (long long)sm_count_mlp() * 8)); }
 
 }  // namespace
@@ -319,9 +457,18 @@ int mlp_forward_run(const void *d_params, const float *d_x, size_t n, int exp_ou
     if (n == 0) return FR_OK;
     const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)n + kFwdThreads - 1) / kFwdThreads,
                                                                        (long long)sm_count_mlp() * 16));
-    mlp_forward_kernel<<<blocks, kFwdThreads, 0, s>>>(static_cast<const __nv_bfloat16 *>(d_params), d_x, (long long)n,
-                                                      exp_out, residual, scale, d_y);
-    FR_CHECK_LAUNCH("mlp_forward_kernel");
+    if (mlp_use_simt()) {
+        mlp_forward_kernel<<<blocks, kFwdThreads, 0, s>>>(static_cast<const __nv_bfloat16 *>(d_params), d_x,
+                                                          (long long)n, exp_out, residual, scale, d_y);
+        FR_CHECK_LAUNCH("mlp_forward_kernel");
+        return FR_OK;
+    }
+    const long long tiles = ((long long)n + 15) / 16;
+    const int mblocks = (int)std::max<long long>(
+        1, std::min<long long>((tiles + kMmaThreads / 32 - 1) / (kMmaThreads / 32), (long long)sm_count_mlp() * 16));
+    mlp_forward_mma_kernel<<<mblocks, kMmaThreads, 0, s>>>(static_cast<const __nv_bfloat16 *>(d_params), d_x,
+                                                          (long long)n, exp_out, residual, scale, d_y);
+    FR_CHECK_LAUNCH("mlp_forward_mma_kernel");
     return FR_OK;
 }
 

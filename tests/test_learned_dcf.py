@@ -123,6 +123,36 @@ def test_gpu_mlp_forward_matches_oracle(oracle):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 15, 16, 17, 1000, 70001])
+def test_gpu_mlp_forward_tensor_cores_vs_fp32_path(oracle, n):
+    """The inference forward (hidden layer on the tensor cores, mma.sync with
+    BF16 operand terms and FP32 accumulation) against the FP32 CUDA-core
+    forward (FR_MLP_SIMT=1) and the FP64 oracle, for sample counts around
+    its 16-sample tiles."""
+    import os
+
+    import torch
+
+    from fastrecon_gb300 import learned_dcf as ld
+    net = ld.DCFNet(_params(5))
+    pf = net.params_bf16_as_float()
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((n, 5)).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    got = net.forward(xt).cpu().numpy()
+    os.environ["FR_MLP_SIMT"] = "1"
+    try:
+        simt = net.forward(xt).cpu().numpy()
+    finally:
+        os.environ.pop("FR_MLP_SIMT")
+    want = oracle.mlp_forward(pf, x)
+    e_tc, e_simt = np.linalg.norm(got - want) / np.linalg.norm(want), np.linalg.norm(simt - want) / np.linalg.norm(want)
+    print(f"n={n}: tensor-core forward vs FP64 {e_tc:.2e}, FP32 CUDA-core forward vs FP64 {e_simt:.2e}")
+    assert e_tc <= TOL_FWD and e_simt <= TOL_FWD
+    assert np.linalg.norm(got - simt) <= 2 * TOL_FWD * np.linalg.norm(want)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 37, 256, 5000])
 @pytest.mark.parametrize("weighted", [False, True])
 def test_gpu_mlp_gradient_matches_oracle(oracle, n, weighted):
