@@ -239,6 +239,39 @@ class Oracle:
         assert rc == 0
         return out
 
+    # -- components with no reference counterpart ---------------------------
+    def deapod_map_f64(self, dim, G, W, lut, recon) -> np.ndarray:
+        """Deapodization map in FP64 (no counterpart in the reference, which
+        does not deapodize).  The kernel's taps around the grid centre
+        c0 = G/2 -- offsets d with dk = |d| < W/2 and weight lut[ki], the
+        reference geometry and LUT index (GridLut.cpp:120-136) -- are
+        transformed to the image: after the backward FFT and fftShift,
+        pixel p holds sum_d w(d) e^{2 pi i (c0 + d).(p - G/2) / G}, whose
+        modulus is |sum_d w(d) cos(2 pi d.(p - G/2) / G)| (the tap set is
+        symmetric).  The map is that modulus over the centred crop (offset
+        (G - R)/2 per axis), divided by its value at the centre pixel,
+        floored at 1e-6.  Returns recon-size float64, x fastest."""
+        hw = np.float32(W) / np.float32(2)
+        reach = int(np.ceil(hw)) + 1
+        taps = []
+        rng = range(-reach, reach + 1)
+        for dz in (rng if dim == 3 else [0]):
+            for dy in rng:
+                for dx in rng:
+                    ki = self.lib.orc_tap_lut_index(float(dx), float(dy), float(dz), float(hw), len(lut))
+                    if ki >= 0:
+                        taps.append((dx, dy, dz, float(lut[ki])))
+        t = np.array(taps, np.float64)
+        R = list(recon) + [1] * (3 - len(recon))
+        off = [(G - R[0]) // 2, (G - R[1]) // 2, (G - R[2]) // 2 if dim == 3 else 0]
+        ax = [2 * np.pi * (np.arange(R[i]) + off[i] - (G // 2 if i < dim else 0)) / G for i in range(3)]
+        out = np.zeros((R[2], R[1], R[0]), np.float64)
+        for dx, dy, dz, w in t:
+            ph = dz * ax[2][:, None, None] + dy * ax[1][None, :, None] + dx * ax[0][None, None, :]
+            out += w * np.cos(ph)
+        m = np.abs(out) / t[:, 3].sum()
+        return np.maximum(m, 1e-6).ravel()
+
     # -- components with no reference counterpart (fr_oracle_ext.c) ---------
     MLP_IN, MLP_HIDDEN = 5, 64
     MLP_PARAMS = 64 * 5 + 64 + 64 * 64 + 64 + 64 + 1

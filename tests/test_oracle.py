@@ -144,3 +144,27 @@ def test_pils_ops_bit_exact(oracle):
         rec = (G // 2, G // 2, G // 2 if dim == 3 else 1)
         got = oracle.sos_map(x, z[key + "_map"], dim, G, rec)
         assert np.array_equal(bits(got.view(np.float32)), bits(z[key + "_sosmap"].view(np.float32))), key
+
+
+def test_deapod_map_oracle_vs_fft(oracle):
+    """The FP64 deapodization map (direct sum over the kernel's taps) equals
+    the backward FFT of the taps seeded at the grid centre, fftShift-ed,
+    cropped and normalised by the centre pixel (numpy FFT in float64)."""
+    for dim, G, R, W, os_ in [(2, 64, 32, 4.0, 2.0), (2, 31, 16, 5.0, 2.0), (3, 24, 16, 4.0, 1.5)]:
+        lut = oracle.kb_lut(W, os_, 512)
+        got = oracle.deapod_map_f64(dim, G, W, lut, (R,) * dim)
+        hw = np.float32(W) / np.float32(2)
+        g = np.zeros((G,) * dim, np.float64)
+        c0 = G // 2
+        reach = int(np.ceil(hw)) + 1
+        for d in np.ndindex(*((2 * reach + 1,) * dim)):
+            d = [x - reach for x in d]
+            dz = d[0] if dim == 3 else 0
+            ki = oracle.lib.orc_tap_lut_index(float(d[-1]), float(d[-2]), float(dz), float(hw), len(lut))
+            if ki >= 0:
+                g[tuple(c0 + x for x in d)] = lut[ki]
+        img = np.fft.fftshift(np.fft.ifftn(g) * g.size)
+        off = (G - R) // 2
+        crop = np.abs(img[(slice(off, off + R),) * dim]) / np.abs(img[(G // 2,) * dim])
+        want = np.maximum(crop, 1e-6).ravel()
+        assert np.max(np.abs(got - want)) < 1e-12, (dim, G)
