@@ -1,8 +1,10 @@
 // GridLut.cpp / cuGridLut.cpp / ConvKernel.cpp -- gridding classes of the C++
 // drop-in API.  Interface: ReconData/GridLut.h:9-42, cuGridLut.h:31-57,
 // ConvKernel.h:7-22.  All gridding runs through the C ABI (fr_plan_*, fr_grid).
+#include <algorithm>
 #include <cstdlib>
 #include <iostream>
+#include <vector>
 
 #include "fastrecon/ConvKernel.h"
 #include "fastrecon/cuGridLut.h"
@@ -114,6 +116,7 @@ void cuGridLut<T>::plan(unsigned reconSize, float overGridFactor, float kWidth, 
     d.coil_group = cg;
     d.flags = FR_PLAN_PRENORMALIZED;
     fr_ok(fr_plan_create(&d, &m_plan), "fr_plan_create");
+    m_grid_cache.reset();
     const auto &traj = m_cuData.cuGetTraj();
     fr_ok(fr_plan_set_trajectory(m_plan, reinterpret_cast<const float *>(traj.data()), traj.size(), nullptr),
           "fr_plan_set_trajectory");
@@ -130,6 +133,14 @@ void cuGridLut<T>::executeInto(cuImageData<T> &img)
 }
 
 // cuGridLut.cu:28-48: all channels in one launch instead of one per channel.
+//
+// Streaming acquisitions (cuReconData.cu:52-62 patches the device k-space
+// and the next execute regrids everything): once the data has seen
+// single-acquisition updates, the grid of each execute() is kept, and the
+// next one grids only dcf * (new - old) of the updated readouts into it
+// (fr_grid_update, which also brings the device k-space up to date), then
+// returns a copy.  Any change of trajectory, DCF, channels or plan makes it
+// a full regrid again.
 template <typename T>
 std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
 {
@@ -141,9 +152,54 @@ std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
     ImageSize size = {G, G, this->m_dim == 3 ? G : 1u};
     auto img = std::make_shared<cuImageData<T>>((int)this->m_dim, size);
     const int C = m_cuData.channels();
-    cuComplexVector<T> buf(img->dataSize() * (std::size_t)C);
+    const std::size_t cells = img->dataSize();
+    cuComplexVector<T> buf(cells * (std::size_t)C);
     img->cuReset((int)this->m_dim, size, C, std::move(buf));
-    executeInto(*img);
+    m_last_incremental = false;
+    if (!m_grid_cache && !m_cuData.cuHasPending()) {
+        executeInto(*img);
+        return img;
+    }
+    const bool valid = m_grid_cache && m_cache_generation == m_cuData.cuGeneration() && m_cache_channels == C &&
+                       m_cuData.cuDeviceChannelsRaw() != nullptr;
+    if (valid) {
+        // group the pending readouts by acquisition: one fr_grid_update per
+        // updated acquisition, with every channel's row (unchanged rows give
+        // a zero change)
+        auto pending = m_cuData.cuTakePending();
+        std::vector<int> acqs;
+        for (const auto &pc : pending) acqs.push_back(pc.first);
+        std::sort(acqs.begin(), acqs.end());
+        acqs.erase(std::unique(acqs.begin(), acqs.end()), acqs.end());
+        const std::size_t ns = (std::size_t)m_cuData.samplesPerAcquisition();
+        cuComplex *kd = m_cuData.cuDeviceChannelsRaw();
+        cuComplexVector<T> fresh(ns * (std::size_t)C);
+        for (int a : acqs) {
+            for (int c = 0; c < C; ++c) {
+                const ComplexVector<T> *host = m_cuData.getChannelData(c);
+                fastrecon::cuda_check(cudaMemcpy(fresh.data() + ns * c, host->data() + ns * a, ns * sizeof(cuComplex),
+                                                 cudaMemcpyHostToDevice),
+                                      "updated acquisition upload");
+            }
+            fr_ok(fr_grid_update(m_plan, reinterpret_cast<float *>(kd), reinterpret_cast<const float *>(fresh.data()),
+                                 ns * (std::size_t)a, ns, reinterpret_cast<const float *>(m_cuData.cuGetDcf().data()),
+                                 C, reinterpret_cast<float *>(m_grid_cache->data()), nullptr),
+                  "fr_grid_update");
+        }
+        m_last_incremental = true;
+    } else {
+        m_grid_cache.reset(new cuComplexVector<T>(cells * (std::size_t)C));
+        fr_ok(fr_grid(m_plan, reinterpret_cast<const float *>(m_cuData.cuGetAllChannels()),
+                      reinterpret_cast<const float *>(m_cuData.cuGetDcf().data()), C,
+                      reinterpret_cast<float *>(m_grid_cache->data()), nullptr),
+              "fr_grid");
+        m_cache_generation = m_cuData.cuGeneration();
+        m_cache_channels = C;
+    }
+    fastrecon::cuda_check(cudaMemcpy(img->cuData(), m_grid_cache->data(), cells * (std::size_t)C * sizeof(cuComplex),
+                                     cudaMemcpyDeviceToDevice),
+                          "grid copy");
+    img->cuMarkModified();
     return img;
 }
 

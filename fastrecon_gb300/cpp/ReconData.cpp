@@ -188,6 +188,8 @@ cuReconData<T>::cuReconData(int samples, int acquisitions) : ReconData<T>(sample
 template <typename T>
 void cuReconData<T>::hostChanged()
 {
+    ++m_generation;
+    m_pending.clear();
     m_cu_traj.reset();
     m_cu_kData.reset();
     m_cu_channels = 0;
@@ -216,10 +218,39 @@ const cuVector<T> &cuReconData<T>::cuGetDcf() const
 }
 
 template <typename T>
+void cuReconData<T>::applyPending() const
+{
+    for (const auto &pc : m_pending) {
+        const std::size_t off = (std::size_t)this->m_samples * pc.first;
+        fastrecon::cuda_check(cudaMemcpy(m_cu_kData->data() + this->m_size * pc.second + off,
+                                         this->m_kDataMultiChannel[pc.second].data() + off,
+                                         (std::size_t)this->m_samples * sizeof(cuComplex), cudaMemcpyHostToDevice),
+                              "acquisition update");
+    }
+    m_pending.clear();
+}
+
+template <typename T>
+std::vector<std::pair<int, int>> cuReconData<T>::cuTakePending()
+{
+    std::vector<std::pair<int, int>> p;
+    p.swap(m_pending);
+    return p;
+}
+
+template <typename T>
+cuComplex *cuReconData<T>::cuDeviceChannelsRaw() const
+{
+    return m_cu_kData && m_cu_channels == this->channels() ? m_cu_kData->data() : nullptr;
+}
+
+template <typename T>
 const cuComplex *cuReconData<T>::cuGetAllChannels() const
 {
     const int C = this->channels();
+    if (m_cu_kData && m_cu_channels == C && !m_pending.empty()) applyPending();
     if (!m_cu_kData || m_cu_channels != C) {
+        m_pending.clear();
         m_views.clear();
         m_cu_kData.reset(new cuComplexVector<T>(this->m_size * (std::size_t)C));
         for (int c = 0; c < C; ++c)
@@ -245,13 +276,12 @@ template <typename T>
 void cuReconData<T>::updateSingleAcquisition(const std::complex<T> *data, int acquisition, int channel)
 {
     ReconData<T>::updateSingleAcquisition(data, acquisition, channel);
-    // cuReconData.cu:52-62: patch the cached device copy too
-    if (m_cu_kData && channel >= 0 && channel < m_cu_channels)
-        fastrecon::cuda_check(cudaMemcpy(m_cu_kData->data() + this->m_size * channel +
-                                             (std::size_t)this->m_samples * acquisition,
-                                         data, (std::size_t)this->m_samples * sizeof(cuComplex),
-                                         cudaMemcpyHostToDevice),
-                              "acquisition update");
+    // cuReconData.cu:52-62 patches the cached device copy at once; here the
+    // readout is recorded and reaches the device copy on the next device
+    // access (cuGetAllChannels) or through an incremental regrid (cuGridLut)
+    if (m_cu_kData && channel >= 0 && channel < m_cu_channels && acquisition >= 0 &&
+        acquisition < this->m_acquisitions)
+        m_pending.emplace_back(acquisition, channel);
 }
 
 template <typename T>
@@ -264,6 +294,7 @@ void cuReconData<T>::clear()
 template <typename T>
 void cuReconData<T>::transformLocalTraj(T translation, T scale)
 {
+    ++m_generation;
     cuTrajVector &traj = getTrajDevice();
     fr_ok(fr_transform_trajectory(reinterpret_cast<float *>(traj.data()), traj.size(), this->rcDim(), translation,
                                   scale, nullptr),

@@ -28,6 +28,10 @@ public:
     void setTiling(int tx, int ty, int tz, int coilGroup);
     // Grid into an existing image whose device buffer holds channels x G^d (no allocation).
     void executeInto(cuImageData<T> &img);
+    // Whether the last execute() regridded only the acquisitions updated
+    // since the one before (ReconData::updateSingleAcquisition) instead of
+    // the whole k-space.
+    bool lastExecuteIncremental() const { return m_last_incremental; }
 
 private:
     cuReconData<T> &m_cuData;
@@ -35,6 +39,12 @@ private:
     int m_gpu_partitions = 1;
     int m_tile[3] = {0, 0, 0};
     int m_coil_group = 0;
+    // streaming acquisitions: the grid of the last execute(), kept once the
+    // data has seen single-acquisition updates
+    std::unique_ptr<cuComplexVector<T>> m_grid_cache;
+    unsigned long long m_cache_generation = 0;
+    int m_cache_channels = 0;
+    bool m_last_incremental = false;
 };
 
 #endif  // FASTRECON_CUGRIDLUT_H

@@ -23,8 +23,23 @@ public:
     // All channels, contiguous on the device.
     const cuComplex *cuGetAllChannels() const;
 
+    // cuReconData.cu:52-62.  With a device copy of the k-space, the readout is
+    // recorded as pending instead of copied at once: a cuGridLut holding the
+    // previous grid then regrids only the change (fr_grid_update), and every
+    // other device access applies the pending readouts first.
     virtual void updateSingleAcquisition(const std::complex<T> *data, int acquisition, int channel = 0) override;
     virtual void clear() override;
+
+    // For incremental regridding (cuGridLut): a counter that changes whenever
+    // the trajectory, DCF or channel set changes (not on single-acquisition
+    // updates); the pending (acquisition, channel) readouts, handed over once
+    // (the caller must then bring the device copy up to date, e.g. through
+    // fr_grid_update); the device k-space without applying them.
+    unsigned long long cuGeneration() const { return m_generation; }
+    bool cuHasPending() const { return !m_pending.empty(); }
+    std::vector<std::pair<int, int>> cuTakePending();
+    cuComplex *cuDeviceChannelsRaw() const;
+    int samplesPerAcquisition() const { return this->m_samples; }
 
 protected:
     void hostChanged() override;
@@ -38,6 +53,9 @@ private:
     mutable int m_cu_channels = 0;
     mutable std::unique_ptr<cuVector<T>> m_cu_dcf;
     mutable std::vector<std::unique_ptr<cuComplexVector<T>>> m_views;
+    unsigned long long m_generation = 0;
+    mutable std::vector<std::pair<int, int>> m_pending;  // (acquisition, channel) not yet on the device
+    void applyPending() const;
 };
 
 #endif  // FASTRECON_CURECONDATA_H
