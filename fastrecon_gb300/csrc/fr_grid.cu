@@ -728,16 +728,15 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
     const unsigned *taps = P.taps;
     const size_t tw = (size_t)P.tap_words;
 
-    // the warp's records: batches of 32 consecutive records, batch b = warp,
-    // warp + kWarps, ...; record k of the warp is lane k % 32 of its batch
-    // k / 32.  Record words past the item read as 0 (no taps).
-    const int nb = (it.count + 31) >> 5;
-    const int nbw = warp < nb ? (nb - warp + kWarps - 1) / kWarps : 0;
-    const int nrec = nbw * 32;
+    // the warp's records: record k of warp w is record w + kWarps k of the
+    // item (every warp within one record of the others); their words are
+    // read 32 at a time, record k from lane k % 32 of batch k / 32.  Words
+    // past the item read as 0 (no taps).
+    const int nrec = warp < it.count ? (it.count - warp + kWarps - 1) / kWarps : 0;
     const unsigned long long *trecs = P.trecs + it.begin;
     auto batch_word = [&](int i) -> unsigned long long {
-        const int j = 32 * (warp + kWarps * i) + lane;
-        return i < nbw && j < it.count ? __ldg(trecs + j) : 0ull;
+        const int k = 32 * i + lane;
+        return k < nrec ? __ldg(trecs + warp + kWarps * k) : 0ull;
     };
     auto fetch = [&](unsigned long long rw, TapStage &st) {
         st.nt = (int)((rw >> 40) & 0xFF);

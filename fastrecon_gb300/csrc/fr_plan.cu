@@ -397,11 +397,24 @@ constexpr int kFillRecMax = 32;  // records per sample (tiles a sample's range t
 
 // cnt[j * kFillThreads], off[j * kFillThreads]: this thread's tap count and
 // first slot word of record j (record-major, so a warp's lanes touch
-// consecutive bytes).
+// consecutive bytes).  XR >= the cells of the range along x: the x loop is
+// unrolled over XR candidates whose dx^2 (or +inf past the range), tile-
+// relative index and tile-local x are computed once per sample.
+template <int XR>
 __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg, const float *c, const int *s,
                                             const int *e, const TileWalk &w, bool place, unsigned char *cnt,
                                             const unsigned char *off, unsigned *slot)
 {
+    float dx2[XR];
+    int jx[XR], lx[XR];
+#pragma unroll
+    for (int i = 0; i < XR; ++i) {
+        const int x = s[0] + i;
+        const float dx = __fsub_rn((float)x, c[0]);
+        dx2[i] = x <= e[0] ? __fmul_rn(dx, dx) : __int_as_float(0x7f800000);
+        jx[i] = tile_div(g, x, 0) - w.lo[0];
+        lx[i] = x - (w.lo[0] + jx[i]) * g.tile[0];
+    }
     float fz = (float)s[2];
     for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
         const float dz = g.dim == 3 ? __fsub_rn(fz, c[2]) : 0.f;
@@ -416,19 +429,16 @@ __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg,
             const int ly = y - (w.lo[1] + jy) * g.tile[1];
             const int jzy = (jz * w.n[1] + jy) * w.n[0];
             const int rowzy = (lz * g.tile[1] + ly) * g.tile[0];
-            float fx = (float)s[0];
-            for (int x = s[0]; x <= e[0]; ++x, fx = __fadd_rn(fx, 1.f)) {
-                const float dx = __fsub_rn(fx, c[0]);
-                const float s2 = __fadd_rn(dzy, __fmul_rn(dx, dx));
+#pragma unroll
+            for (int i = 0; i < XR; ++i) {
+                const float s2 = __fadd_rn(dzy, dx2[i]);
                 if (s2 < tg.smax) {
-                    const int jx = tile_div(g, x, 0) - w.lo[0];
-                    const int j = (jzy + jx) * kFillThreads;
+                    const int j = (jzy + jx[i]) * kFillThreads;
                     const int k = cnt[j]++;
                     if (place) {
                         const int wi = off[j] + k;
-                        const int lx = x - (w.lo[0] + jx) * g.tile[0];
                         if (wi < tg.words)
-                            slot[wi] = (unsigned)(rowzy + lx) |
+                            slot[wi] = (unsigned)(rowzy + lx[i]) |
                                        ((unsigned)tap_lut_index(s2, tg.lut_e, tg.kc, tg.L) << kTapCellBits);
                     }
                 }
@@ -437,6 +447,7 @@ __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg,
     }
 }
 
+template <int XR>
 __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *__restrict__ traj, size_t n,
                                                                  BinGeom g, TapGeom tg,
                                                                  const long long *__restrict__ stripe_base,
@@ -469,7 +480,7 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
         }
         // taps per record, then each record's first word, then the taps
         for (int j = 0; j < cnt_t; ++j) cnt[j * kFillThreads] = 0;
-        if (cnt_t > 0) sample_taps(g, tg, c, s, e, w, false, cnt, off, mine);
+        if (cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, false, cnt, off, mine);
         int tot = 0;
         for (int j = 0; j < cnt_t; ++j) {
             off[j * kFillThreads] = (unsigned char)min(tot, 255);
@@ -477,7 +488,7 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
             cnt[j * kFillThreads] = 0;
         }
         if (tot > tg.words) *tg.err = FR_ERR_CAPACITY;  // never: the slot bounds every sample's taps
-        if (cnt_t > 0) sample_taps(g, tg, c, s, e, w, true, cnt, off, mine);
+        if (cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, true, cnt, off, mine);
 
         const int stripe = stripe_of(base + threadIdx.x - lane);
         int maxcnt = __reduce_max_sync(0xffffffffu, cnt_t);
@@ -503,20 +514,37 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
         // the block's slots are words [base * words, (base + nv) * words):
         // 16-byte aligned (base is a multiple of kFillThreads), copied as uint4
         const int nv = (int)min((size_t)kFillThreads, n - base);
-        const int total = nv * tg.words;
-        uint4 *dst = reinterpret_cast<uint4 *>(tg.taps + base * (size_t)tg.words);
-        for (int qd = threadIdx.x; qd < total / 4; qd += kFillThreads) {
-            unsigned v[4];
+        const int W = tg.words, total = nv * W;
+        uint4 *dst = reinterpret_cast<uint4 *>(tg.taps + base * (size_t)W);
+        {
+            // word wi = 4 qd + k of the block's slots is word (wi mod W) of
+            // sample wi / W: kept as a (sample, word) pair advanced without
+            // divisions (one division to start, then steps of 4 kFillThreads)
+            const int step = 4 * kFillThreads, sq = step / W, sr = step - sq * W;
+            int smp = (4 * threadIdx.x) / W, wd = 4 * threadIdx.x - smp * W;
+            for (int qd = threadIdx.x; qd < total / 4; qd += kFillThreads) {
+                unsigned v[4];
+                int sm = smp, wk = wd;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int wi = 4 * qd + k, smp = wi / tg.words;
-                v[k] = stage[smp * S + (wi - smp * tg.words)];
+                for (int k = 0; k < 4; ++k) {
+                    v[k] = stage[sm * S + wk];
+                    if (++wk == W) {
+                        wk = 0;
+                        ++sm;
+                    }
+                }
+                dst[qd] = make_uint4(v[0], v[1], v[2], v[3]);
+                smp += sq;
+                wd += sr;
+                if (wd >= W) {
+                    wd -= W;
+                    ++smp;
+                }
             }
-            dst[qd] = make_uint4(v[0], v[1], v[2], v[3]);
         }
         for (int wi = (total & ~3) + threadIdx.x; wi < total; wi += kFillThreads) {
-            const int smp = wi / tg.words;
-            tg.taps[base * (size_t)tg.words + wi] = stage[smp * S + (wi - smp * tg.words)];
+            const int smp = wi / W;
+            tg.taps[base * (size_t)W + wi] = stage[smp * S + (wi - smp * W)];
         }
         __syncthreads();
     }
@@ -814,7 +842,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         const int F = (int)std::floor(2.0 * p->hw) + 1;
         int recmax = 1;
         for (int d = 0; d < p->dim; ++d) recmax *= (F - 1 + p->tile[d] - 1) / p->tile[d] + 1;
-        if (words <= kTapRecMax && recmax <= kFillRecMax && !p->taps.reserve(n * (size_t)words * 4) &&
+        if (words <= kTapRecMax && recmax <= kFillRecMax && F <= 9 && !p->taps.reserve(n * (size_t)words * 4) &&
             !p->trecs.reserve(std::max<long long>(tot.pairs, 1) * 8))
             p->tap_words = words;
     }
@@ -829,9 +857,12 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         tg.words = p->tap_words;
         tg.err = p->err_dev;
         const size_t smem = (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * kFillRecMax);
+        // cells of a sample's range along x: at most floor(2 hw) + 1
+        auto kern = (int)std::floor(2.0 * p->hw) + 1 <= 5 ? fill_taps_kernel<5> : fill_taps_kernel<9>;
+        if ((int)std::floor(2.0 * p->hw) + 1 > 9) return fail(FR_ERR_UNSUPPORTED, "tap lists: kernel too wide");
         if (smem > 48 * 1024)
-            FR_CUDA(cudaFuncSetAttribute(fill_taps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        fill_taps_kernel<<<grid_blocks(n, kFillThreads), kFillThreads, smem, s>>>(
+            FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid_blocks(n, kFillThreads), kFillThreads, smem, s>>>(
             traj, n, g, tg, p->stripe_base.as<long long>(), p->tile_fill.as<int>(), p->pairs.as<unsigned long long>());
         FR_CHECK_LAUNCH("fill_taps_kernel");
     } else if (n > 0) {
