@@ -683,7 +683,8 @@ struct TapStage {
     float v;
 };
 
-template <int R>
+// IT: index type of the tap words and values (32-bit when every index fits).
+template <int R, typename IT>
 __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 {
     extern __shared__ float4 smem_raw[];
@@ -734,27 +735,39 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
     // past the item read as 0 (no taps).
     const int nrec = warp < it.count ? (it.count - warp + kWarps - 1) / kWarps : 0;
     const unsigned long long *trecs = P.trecs + it.begin;
-    auto batch_word = [&](int i) -> unsigned long long {
-        const int k = 32 * i + lane;
-        return k < nrec ? __ldg(trecs + warp + kWarps * k) : 0ull;
+    // a batch of 32 records, one per lane, as index of the lane's record's
+    // first tap word, index of its coil group's values, tap count
+    struct Batch {
+        IT tb, vo;
+        int nt;
     };
-    auto fetch = [&](unsigned long long rw, TapStage &st) {
-        st.nt = (int)((rw >> 40) & 0xFF);
-        const size_t base = (size_t)(unsigned)rw * tw + (size_t)((rw >> 32) & 0xFF);
-        st.t0 = lane < st.nt ? __ldg(taps + base + lane) : 0u;
-        st.t1 = lane + 32 < st.nt ? __ldg(taps + base + lane + 32) : 0u;
-        st.v = vlane && st.nt ? __ldg(kt + 2 * (size_t)(unsigned)rw * (size_t)P.kstride) : 0.f;
+    auto load_batch = [&](int i) -> Batch {
+        const int k = 32 * i + lane;
+        const unsigned long long rw = k < nrec ? __ldg(trecs + warp + kWarps * k) : 0ull;
+        Batch b;
+        b.nt = (int)((rw >> 40) & 0xFF);
+        b.tb = (IT)(unsigned)rw * (IT)tw + (IT)((rw >> 32) & 0xFF);
+        b.vo = (IT)(unsigned)rw * (IT)(2 * P.kstride);
+        return b;
+    };
+    auto fetch = [&](const Batch &b, int src_lane, TapStage &st) {
+        st.nt = __shfl_sync(0xffffffffu, b.nt, src_lane);
+        const IT tb = __shfl_sync(0xffffffffu, b.tb, src_lane);
+        const IT vo = __shfl_sync(0xffffffffu, b.vo, src_lane);
+        st.t0 = lane < st.nt ? __ldg(taps + tb + (IT)lane) : 0u;
+        st.t1 = lane + 32 < st.nt ? __ldg(taps + tb + (IT)(lane + 32)) : 0u;
+        st.v = vlane && st.nt ? __ldg(kt + vo) : 0.f;
     };
 
-    unsigned long long cur = batch_word(0), nxt = batch_word(1);
+    Batch cur = load_batch(0), nxt = load_batch(1);
     TapStage st[kTapDepth];
 #pragma unroll
-    for (int d = 0; d < kTapDepth; ++d) fetch(__shfl_sync(0xffffffffu, cur, d), st[d]);
+    for (int d = 0; d < kTapDepth; ++d) fetch(cur, d, st[d]);
 
     for (int k0 = 0; k0 < nrec; k0 += kTapDepth) {
         if (k0 > 0 && (k0 & 31) == 0) {
             cur = nxt;
-            nxt = batch_word((k0 >> 5) + 1);
+            nxt = load_batch((k0 >> 5) + 1);
         }
 #pragma unroll
         for (int d = 0; d < kTapDepth; ++d) {
@@ -786,13 +799,13 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
             // refill this stage with record k + kTapDepth
             const int k2 = k + kTapDepth;
             if (k2 < nrec) {
-                const unsigned long long src = (k2 >> 5) == (k0 >> 5) ? cur : nxt;
-                fetch(__shfl_sync(0xffffffffu, src, k2 & 31), st[d]);
+                fetch((k2 >> 5) == (k0 >> 5) ? cur : nxt, k2 & 31, st[d]);
             } else {
                 st[d].nt = 0;
             }
             if (ntap > 0) {
                 if (NG == 1) {
+#pragma unroll 2
                     for (int m = 0; m < np; m += 2) {
                         const int4 e = lds_s32x4(list + 8u * (unsigned)m);
                         red_add_fx((unsigned)e.x ^ f0b, __int_as_float(e.y), vs);
@@ -1067,7 +1080,10 @@ int launch_taps(fr_plan p, const GridParams &P, long long nitems, long long nspl
     const TapSmem m = tap_smem_layout(P.K, R, P.L);
     const size_t smem = m.end + 128;
     if (smem > 227 * 1024) return fail(FR_ERR_UNSUPPORTED, "tap-list scatter does not fit in shared memory");
-    auto kern = grid_taps_kernel<R>;
+    // 32-bit indices when the tap words and sample-major values allow them
+    const bool idx32 = (double)P.n * (double)P.tap_words < 2147483647.0 &&
+                       (double)P.n * (double)(2 * P.kstride) < 2147483647.0;
+    auto kern = idx32 ? grid_taps_kernel<R, unsigned> : grid_taps_kernel<R, unsigned long long>;
     if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)nitems, (unsigned)P.ngroups);
     cudaEvent_t *ev = nullptr;
