@@ -425,8 +425,10 @@ int fr_recon_run_host(fr_recon r, const float *h_traj, const float *h_dcf, const
  * run): queues the upload of the inputs, the recon on `stream` and the
  * download of the image, and returns without waiting.  Two device staging
  * slots alternate, so the upload of one volume and the download of the
- * previous image overlap the recon of the one in between.  The host buffers
- * (pinned for overlap) must stay valid and unchanged until fr_recon_sync
+ * previous image overlap the recon of the one in between.  The copies may
+ * still be reading h_traj, h_dcf and h_kdata, and writing h_image, after this
+ * call returns: every one of these host buffers (pinned for overlap) must
+ * stay valid, the inputs unmodified, and h_image unread, until fr_recon_sync
  * returns; the images are fr_recon_run_host's. */
 int fr_recon_submit_host(fr_recon r, const float *h_traj, const float *h_dcf, const float *h_kdata,
                          size_t n, float *h_image, void *stream);
