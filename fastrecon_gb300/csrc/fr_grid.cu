@@ -1135,6 +1135,27 @@ void default_tiling(int dim, int *tile, int *coil_group, int channels)
     }
 }
 
+int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s)
+{
+    p->kt_prepared = nullptr;
+    if (p->n == 0) return FR_OK;
+    const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
+    if (trsmem > 96 * 1024) return fail(FR_ERR_UNSUPPORTED, "too many channels for the sample-major copy");
+    const int cstride = channels + (channels & 1);  // even: rows start on 16-byte boundaries
+    if (p->kt.reserve(p->n * (size_t)cstride * sizeof(float2)) || p->kmag.reserve(p->n * sizeof(float)))
+        return FR_ERR_OUT_OF_MEMORY;
+    if (trsmem > 48 * 1024)
+        FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)trsmem));
+    transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
+        reinterpret_cast<const float2 *>(d_kdata), d_dcf, p->kt.as<float2>(), p->kmag.as<float>(), (long long)p->n,
+        channels, cstride);
+    FR_CHECK_LAUNCH("transpose_kspace_kernel");
+    p->kt_prepared = d_kdata;
+    p->kt_prepared_channels = channels;
+    return FR_OK;
+}
+
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
              cudaStream_t s, bool skip_empty)
 {
@@ -1187,15 +1208,13 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     const bool taps = p->tap_words > 0 && R <= 32;
     if (p->kspace_sample_major && (channels >= 4 || taps) && p->n > 0 && trsmem <= 96 * 1024) {
         const int cstride = channels + (channels & 1);  // even: rows start on 16-byte boundaries
-        if (p->kt.reserve(p->n * (size_t)cstride * sizeof(float2)) || p->kmag.reserve(p->n * sizeof(float)))
-            return FR_ERR_OUT_OF_MEMORY;
-        if (trsmem > 48 * 1024)
-            FR_CUDA(cudaFuncSetAttribute(transpose_kspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)trsmem));
-        transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
-            reinterpret_cast<const float2 *>(d_kdata), d_dcf, p->kt.as<float2>(), p->kmag.as<float>(),
-            (long long)p->n, channels, cstride);
-        FR_CHECK_LAUNCH("transpose_kspace_kernel");
+        const bool ready = p->kt_prepared == d_kdata && p->kt_prepared_channels == channels;
+        p->kt_prepared = nullptr;
+        if (!ready) {
+            const int st = kspace_prepare(p, d_kdata, d_dcf, channels, s);
+            p->kt_prepared = nullptr;
+            if (st) return st;
+        }
         P.kdata = p->kt.as<float>();
         P.sample_major = 1;
         P.mag = p->kmag.as<float>();

@@ -112,6 +112,8 @@ struct fr_plan_s {
     fr::DevBuf small;         // 256 bytes of scratch (feature max |k|)
     fr::DevBuf kt;            // n x channels complex: sample-major copy of dcf * k-space (fr_grid)
     fr::DevBuf kmag;          // n floats: per sample max |re|, |im| of dcf * k over the coils
+    const float *kt_prepared = nullptr;  // k-space whose copy kspace_prepare made for the next grid_run
+    int kt_prepared_channels = 0;
     fr::DevBuf tile_mask;     // ntiles bits: tile holds bin records (recon path skips the others)
     bool kspace_sample_major = true;  // cleared by FR_KSPACE_COIL_MAJOR=1
 
@@ -144,6 +146,11 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
 // caller's next reader masks them with the plan's tile bitmap).
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
              cudaStream_t s, bool skip_empty = false);
+// The scatter's sample-major dcf * k-space copy, made ahead of grid_run
+// (e.g. on another stream while the plan's kernels run); the next grid_run
+// with the same k-space pointer and channel count uses it instead of making
+// its own.  The caller orders that grid_run after this copy.
+int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s);
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
 // sos_mode: 2 = the whole SoS (sqrt, / deapod); for coils in slabs 0 = store
 // the plain sum of |x|^2, | 1 = add to the sum already in d_out.

@@ -447,103 +447,8 @@ __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg,
     }
 }
 
-// The same placement when the sample's cell range touches at most 2 tiles
-// along each axis (tiles at least the kernel footprint): a first walk only
-// tests validity and records, per axis, which of the sample's taps (in
-// walk order z, y, x) lie in the upper tile (bitmasks mz, my, mx); the taps
-// of record (jz, jy, jx) are then a mask of those bits, its run starts after
-// the taps of every record before it in the tile walk (x fastest), and a
-// second walk writes each tap at that start plus the count of its record's
-// taps before it.  No per-tap counters.  Returns the sample's tap count.
 template <int XR>
-__device__ __forceinline__ int sample_taps2(const BinGeom &g, const TapGeom &tg, const float *c, const int *s,
-                                            const int *e, const TileWalk &w, unsigned *slot,
-                                            unsigned long long &mz_out, unsigned long long &my_out,
-                                            unsigned long long &mx_out)
-{
-    // first cell of the upper tile along each axis (past the range if one tile)
-    const int bx = w.n[0] > 1 ? (w.lo[0] + 1) * g.tile[0] : 1 << 30;
-    const int by = w.n[1] > 1 ? (w.lo[1] + 1) * g.tile[1] : 1 << 30;
-    const int bz = w.n[2] > 1 ? (w.lo[2] + 1) * g.tile[2] : 1 << 30;
-    float dx2[XR];
-#pragma unroll
-    for (int i = 0; i < XR; ++i) {
-        const int x = s[0] + i;
-        const float dx = __fsub_rn((float)x, c[0]);
-        dx2[i] = x <= e[0] ? __fmul_rn(dx, dx) : __int_as_float(0x7f800000);
-    }
-    unsigned long long mz = 0, my = 0, mx = 0;
-    int t = 0;
-    {
-        float fz = (float)s[2];
-        for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
-            const float dz = g.dim == 3 ? __fsub_rn(fz, c[2]) : 0.f;
-            const float dz2 = __fmul_rn(dz, dz);
-            float fy = (float)s[1];
-            for (int y = s[1]; y <= e[1]; ++y, fy = __fadd_rn(fy, 1.f)) {
-                const float dy = __fsub_rn(fy, c[1]);
-                const float dzy = __fadd_rn(dz2, __fmul_rn(dy, dy));
-                const bool uz = z >= bz, uy = y >= by;
-#pragma unroll
-                for (int i = 0; i < XR; ++i) {
-                    if (__fadd_rn(dzy, dx2[i]) < tg.smax) {
-                        const unsigned long long b = 1ull << t;
-                        if (uz) mz |= b;
-                        if (uy) my |= b;
-                        if (s[0] + i >= bx) mx |= b;
-                        ++t;
-                    }
-                }
-            }
-        }
-    }
-    const int ntot = t;
-    mz_out = mz;
-    my_out = my;
-    mx_out = mx;
-    if (ntot > tg.words) return ntot;  // never: the slot bounds every sample's taps
-    const unsigned long long all = ntot >= 64 ? ~0ull : (1ull << ntot) - 1ull;
-    t = 0;
-    float fz = (float)s[2];
-    for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
-        const float dz = g.dim == 3 ? __fsub_rn(fz, c[2]) : 0.f;
-        const float dz2 = __fmul_rn(dz, dz);
-        const int jz = z >= bz ? 1 : 0;
-        const int lz = z - (w.lo[2] + jz) * g.tile[2];
-        float fy = (float)s[1];
-        for (int y = s[1]; y <= e[1]; ++y, fy = __fadd_rn(fy, 1.f)) {
-            const float dy = __fsub_rn(fy, c[1]);
-            const float dzy = __fadd_rn(dz2, __fmul_rn(dy, dy));
-            const int jy = y >= by ? 1 : 0;
-            const int ly = y - (w.lo[1] + jy) * g.tile[1];
-            const int rowzy = (lz * g.tile[1] + ly) * g.tile[0];
-            // for both x tiles of this row: the taps of records before it and its own
-            const unsigned long long zlt = jz ? all & ~mz : 0ull, zeq = jz ? mz : all & ~mz;
-            const unsigned long long ylt = jy ? all & ~my : 0ull, yeq = jy ? my : all & ~my;
-            const unsigned long long zy = zeq & yeq;
-            const unsigned long long pre0 = zlt | (zeq & ylt), own0 = zy & ~mx;  // lower x tile
-            const unsigned long long pre1 = pre0 | own0, own1 = zy & mx;           // upper x tile
-#pragma unroll
-            for (int i = 0; i < XR; ++i) {
-                const float s2 = __fadd_rn(dzy, dx2[i]);
-                if (s2 < tg.smax) {
-                    const int x = s[0] + i;
-                    const int jx = x >= bx ? 1 : 0;
-                    const unsigned long long below = (1ull << t) - 1ull;
-                    const int pos = __popcll(jx ? pre1 : pre0) + __popcll((jx ? own1 : own0) & below);
-                    const int lx = x - (w.lo[0] + jx) * g.tile[0];
-                    slot[pos] = (unsigned)(rowzy + lx) |
-                                ((unsigned)tap_lut_index(s2, tg.lut_e, tg.kc, tg.L) << kTapCellBits);
-                    ++t;
-                }
-            }
-        }
-    }
-    return ntot;
-}
-
-template <int XR, bool FAST>
-__global__ void __launch_bounds__(kFillThreads, 2) fill_taps_kernel(const float4 *__restrict__ traj, size_t n,
+__global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *__restrict__ traj, size_t n,
                                                                  BinGeom g, TapGeom tg,
                                                                  const long long *__restrict__ stripe_base,
                                                                  int *__restrict__ tile_fill,
@@ -573,32 +478,16 @@ __global__ void __launch_bounds__(kFillThreads, 2) fill_taps_kernel(const float4
             w.lo[0] = w.lo[1] = w.lo[2] = 0;
             w.n[0] = w.n[1] = w.n[2] = 1;
         }
+        // taps per record, then each record's first word, then the taps
         int tot = 0;
-        if (FAST) {
-            // at most 8 records: counts and run starts from the records' tap
-            // masks, record j = (jz n1 + jy) n0 + jx in walk order
-            unsigned long long mz = 0, my = 0, mx = 0;
-            if (cnt_t > 0) tot = sample_taps2<XR>(g, tg, c, s, e, w, mine, mz, my, mx);
-            const unsigned long long all = tot >= 64 ? ~0ull : (1ull << tot) - 1ull;
-            int o = 0;
-            for (int j = 0; j < cnt_t; ++j) {
-                const int jx = j % w.n[0], jy = (j / w.n[0]) % w.n[1], jz = j / (w.n[0] * w.n[1]);
-                const int nj = __popcll((jz ? mz : all & ~mz) & (jy ? my : all & ~my) & (jx ? mx : all & ~mx));
-                off[j * kFillThreads] = (unsigned char)min(o, 255);
-                cnt[j * kFillThreads] = (unsigned char)nj;
-                o += nj;
-            }
-        } else {
-            // taps per record, then each record's first word, then the taps
-            for (int j = 0; j < cnt_t; ++j) cnt[j * kFillThreads] = 0;
-            if (cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, false, cnt, off, mine);
-            for (int j = 0; j < cnt_t; ++j) {
-                off[j * kFillThreads] = (unsigned char)min(tot, 255);
-                tot += cnt[j * kFillThreads];
-                cnt[j * kFillThreads] = 0;
-            }
-            if (tot <= tg.words && cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, true, cnt, off, mine);
+        for (int j = 0; j < cnt_t; ++j) cnt[j * kFillThreads] = 0;
+        if (cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, false, cnt, off, mine);
+        for (int j = 0; j < cnt_t; ++j) {
+            off[j * kFillThreads] = (unsigned char)min(tot, 255);
+            tot += cnt[j * kFillThreads];
+            cnt[j * kFillThreads] = 0;
         }
+        if (tot <= tg.words && cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, true, cnt, off, mine);
         if (tot > tg.words) *tg.err = FR_ERR_CAPACITY;  // never: the slot bounds every sample's taps
 
         const int stripe = stripe_of(base + threadIdx.x - lane);
@@ -972,10 +861,7 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         // mask walk when a range touches at most 2 tiles per axis and its
         // taps fit one 64-bit mask
         const int Fx = (int)std::floor(2.0 * p->hw) + 1;
-        bool fast = p->tap_words <= 64;
-        for (int d = 0; d < p->dim; ++d) fast = fast && (Fx - 1 + p->tile[d] - 1) / p->tile[d] + 1 <= 2;
-        auto kern = Fx <= 5 ? (fast ? fill_taps_kernel<5, true> : fill_taps_kernel<5, false>)
-                            : (fast ? fill_taps_kernel<9, true> : fill_taps_kernel<9, false>);
+        auto kern = Fx <= 5 ? fill_taps_kernel<5> : fill_taps_kernel<9>;
         if ((int)std::floor(2.0 * p->hw) + 1 > 9) return fail(FR_ERR_UNSUPPORTED, "tap lists: kernel too wide");
         if (smem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -38,6 +38,10 @@ struct fr_recon_s {
     // trajectory is planned
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_start = nullptr, copy_done = nullptr;
+    // the scatter's sample-major k-space copy is made on its own stream while
+    // the plan's tap fill runs (one reads and writes HBM, the other computes)
+    cudaStream_t prep_stream = nullptr;
+    cudaEvent_t prep_start = nullptr, prep_done = nullptr;
     // submitted host-buffer volumes (fr_recon_submit_host): two staging
     // slots, so volume i + 1 uploads while volume i is reconstructed and
     // volume i - 1's image downloads
@@ -63,6 +67,10 @@ struct fr_recon_s {
         if (copy_start) cudaEventDestroy(copy_start);
         if (copy_done) cudaEventDestroy(copy_done);
         if (copy_stream) cudaStreamDestroy(copy_stream);
+        if (prep_stream) cudaStreamSynchronize(prep_stream);
+        if (prep_stream) cudaStreamDestroy(prep_stream);
+        if (prep_start) cudaEventDestroy(prep_start);
+        if (prep_done) cudaEventDestroy(prep_done);
         if (plan) fr_plan_destroy(plan);
         if (fft) fr_fft_destroy(fft);
         if (fft1) fr_fft_destroy(fft1);
@@ -184,6 +192,22 @@ int recon_run(fr_recon r, const float *d_traj, const float *d_dcf, const float *
     float *g = r->grid.as<float>();
     if (r->timing) cudaEventRecord(r->ev[0], s);
     st = fr_plan_set_trajectory(r->plan, d_traj, n, stream);
+    // the first slab's sample-major k-space copy, on the side stream while
+    // the plan's last kernels run on `s` (after everything before them)
+    const int slab0 = std::min(r->slab, r->d.channels);
+    if (!st && n > 0 && r->plan->tap_words > 0 && !r->timing) {
+        if (!r->prep_stream) {
+            FR_CUDA(cudaStreamCreateWithFlags(&r->prep_stream, cudaStreamNonBlocking));
+            FR_CUDA(cudaEventCreateWithFlags(&r->prep_start, cudaEventDisableTiming));
+            FR_CUDA(cudaEventCreateWithFlags(&r->prep_done, cudaEventDisableTiming));
+        }
+        FR_CUDA(cudaEventRecord(r->prep_start, s));
+        FR_CUDA(cudaStreamWaitEvent(r->prep_stream, r->prep_start, 0));
+        if (kdata_ready) FR_CUDA(cudaStreamWaitEvent(r->prep_stream, kdata_ready, 0));
+        st = kspace_prepare(r->plan, d_kdata, d_dcf, slab0, r->prep_stream);
+        if (!st) FR_CUDA(cudaEventRecord(r->prep_done, r->prep_stream));
+        if (!st) FR_CUDA(cudaStreamWaitEvent(s, r->prep_done, 0));
+    }
     if (r->timing) cudaEventRecord(r->ev[1], s);
     if (!st && kdata_ready) {
         cudaError_t e = cudaStreamWaitEvent(s, kdata_ready, 0);
