@@ -41,11 +41,26 @@ void DevBuf::release()
     bytes = 0;
 }
 
+// Host-side fault injection for the out-of-memory paths: with
+// FR_FAIL_ALLOC_BYTES=B in the environment, every device reservation of B
+// bytes or more fails as cudaMalloc would (nothing is allocated).
+static bool injected_alloc_failure(size_t want)
+{
+    const char *v = std::getenv("FR_FAIL_ALLOC_BYTES");
+    if (!v || !*v) return false;
+    const unsigned long long b = std::strtoull(v, nullptr, 10);
+    return b > 0 && want >= b;
+}
+
 int DevBuf::reserve(size_t n)
 {
     if (n <= bytes && ptr) return 0;
     release();
     size_t want = std::max<size_t>(n, 256);
+    if (injected_alloc_failure(want)) {
+        fail(FR_ERR_OUT_OF_MEMORY, "device allocation refused (FR_FAIL_ALLOC_BYTES)");
+        return 1;
+    }
     cudaError_t e = cudaMalloc(&ptr, want);
     if (e != cudaSuccess) {
         ptr = nullptr;

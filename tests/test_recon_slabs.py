@@ -35,6 +35,26 @@ def test_slabs_equal_single_pass(name, mode):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small", "radial2d_oddgrid", "koosh3d_odd"])
+@pytest.mark.parametrize("coils_per_slab", [1, 2])
+def test_slabs_vs_oracle(oracle, name, coils_per_slab):
+    """Coils in slabs against the oracle's image (the reference pipeline,
+    Program/Main.cpp:101-181) at the recon bar 1e-5, with and without the
+    pruned register FFT."""
+    import torch
+    c = load_case(name)
+    cells = c["G"] ** c["dim"]
+    rec = (c["recon"],) * 2 + ((c["recon"] if c["dim"] == 3 else 1),)
+    want = oracle.recon(c["traj"], c["dcf"], c["kdata"], c["dim"], c["recon"], c["os"], c["W"], c["L"], rec,
+                        threads=2)
+    for mode in (dict(), dict(use_cufft=True)):
+        got = _run(torch, c, coils_per_slab * cells * 8, **mode)
+        err = rel_l2(got, want)
+        print(f"{name} {mode} {coils_per_slab} coil(s) per slab: image vs oracle rel-L2 {err:.2e}")
+        assert err <= 1e-5
+
+
+@pytest.mark.gpu
 def test_slab_budget_smaller_than_one_coil_still_runs():
     import torch
     c = load_case("radial2d_small")

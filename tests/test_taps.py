@@ -107,3 +107,36 @@ def test_tap_lists_repeatable(torch):
     p, g1 = _grid(torch, c, c["kdata"], chunk=512)
     g2 = p.grid(torch.from_numpy(c["kdata"]).cuda(), torch.from_numpy(c["dcf"]).cuda()).cpu().numpy()
     assert rel_l2(g1, g2) <= 1e-6
+
+
+def test_out_of_memory_paths_with_injected_failures(torch):
+    """Host-side fault injection (FR_FAIL_ALLOC_BYTES: device reservations of
+    that many bytes or more fail as cudaMalloc would).  A plan whose tap lists
+    cannot be allocated falls back to the geometry scatter and stays correct;
+    a plan that cannot hold the trajectory returns FR_ERR_OUT_OF_MEMORY (3)
+    from fr_plan_set_trajectory, and so does a recon object's creation; with
+    the injection removed the same calls succeed."""
+    import os
+
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300.capi import FastreconError
+    c = load_case("koosh3d_small")
+    n = c["traj"].shape[0]
+    try:
+        os.environ["FR_FAIL_ALLOC_BYTES"] = str(n * 30 * 4)  # below the tap slots, above everything else
+        p, g = _grid(torch, c, c["kdata"])
+        assert p.tap_words() == 0
+        assert rel_l2(g, c["grid"]) <= TOL
+        os.environ["FR_FAIL_ALLOC_BYTES"] = str(n * 8)  # below the trajectory copy
+        p = fr.GridPlan(c["dim"], c["G"], c["W"], lut=c["lut"])
+        with pytest.raises(FastreconError) as ei:
+            p.set_trajectory(torch.from_numpy(c["traj"]).cuda())
+        assert ei.value.status == 3
+        os.environ["FR_FAIL_ALLOC_BYTES"] = "64"
+        with pytest.raises(FastreconError) as ei:
+            fr.Recon(c["dim"], c["recon"], c["os"], c["coils"], max_samples=n)
+        assert ei.value.status == 3
+    finally:
+        os.environ.pop("FR_FAIL_ALLOC_BYTES", None)
+    p, g = _grid(torch, c, c["kdata"])
+    assert p.tap_words() > 0 and rel_l2(g, c["grid"]) <= TOL
