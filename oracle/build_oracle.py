@@ -99,5 +99,12 @@ def clean() -> None:
 
 
 if __name__ == "__main__":
-    print(build_oracle(force="--force" in sys.argv))
-    print(build_ref(force="--force" in sys.argv))
+    import argparse
+    ap = argparse.ArgumentParser(description="build the CPU oracle and, where the reference checkout exists, "
+                                             "the reference's own CPU sources")
+    ap.add_argument("--reference", default=None,
+                    help="reference checkout (default: $FASTRECON_REF_ROOT, else the build machine's checkout)")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args()
+    print(build_oracle(force=a.force))
+    print(build_ref(ref_root=a.reference, force=a.force))
