@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libfastrecon_gb300.so")
 
 FR_PLAN_CHECKERBOARD = 1
 FR_PLAN_NO_TAP_LISTS = 4
+FR_PLAN_ACCUMULATE = 8
 FR_RECON_DEAPODIZE = 1
 FR_RECON_CUFFT = 2
 FR_RECON_PRUNED_FFT = 4
@@ -64,6 +65,7 @@ _SIGS = {
     "fr_plan_profile_read": (C.c_int, [_VP, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "fr_kernel_launches": (C.c_longlong, []),
     "fr_grid": (C.c_int, [_VP, _VP, _VP, C.c_int, _VP, _VP]),
+    "fr_grid_partitioned": (C.c_int, [C.POINTER(PlanDesc), _VP, C.c_size_t, _VP, _VP, C.c_int, _VP, C.c_size_t, _VP]),
     "fr_grid_noalloc": (C.c_int, [_VP, C.c_size_t, C.c_int, C.c_uint, C.c_float, C.POINTER(C.c_float), C.c_int,
                                   _VP, _VP, C.c_int, _VP, _VP]),
     "fr_batch_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(_VP)]),

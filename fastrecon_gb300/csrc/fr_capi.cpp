@@ -444,6 +444,45 @@ int fr_grid(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, f
     return grid_run(p, d_kdata, d_dcf, channels, d_grid, (cudaStream_t)stream);
 }
 
+int fr_grid_partitioned(const fr_plan_desc *desc, const float *d_traj, size_t n, const float *d_kdata,
+                        const float *d_dcf, int channels, float *d_grid, size_t partition, void *stream)
+{
+    if (!desc || !d_grid || (n && (!d_traj || !d_kdata || !d_dcf)) || channels < 1)
+        return fail(FR_ERR_INVALID_ARGUMENT, "null argument");
+    if (desc->dim != 2 && desc->dim != 3) return fail(FR_ERR_INVALID_ARGUMENT, "dim must be 2 or 3");
+    if ((reinterpret_cast<uintptr_t>(d_kdata) & 7) || (reinterpret_cast<uintptr_t>(d_grid) & 7))
+        return fail(FR_ERR_INVALID_ARGUMENT, "complex buffers must be 8-byte aligned");
+    if (reinterpret_cast<uintptr_t>(d_traj) & 15) return fail(FR_ERR_INVALID_ARGUMENT, "trajectory must be 16-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t G = desc->grid_size;
+    const size_t cells = desc->dim == 3 ? G * G * G : G * G;
+    if (partition == 0 || partition > n) partition = n;
+
+    fr_plan_desc d = *desc;
+    d.flags |= FR_PLAN_PRENORMALIZED | FR_PLAN_ACCUMULATE;
+    fr_plan plan = nullptr;
+    int st = fr_plan_create(&d, &plan);
+    if (st) return st;
+    float *tn = nullptr;
+    if (n && cudaMallocAsync(reinterpret_cast<void **>(&tn), n * 4 * sizeof(float), s) != cudaSuccess) {
+        cudaGetLastError();
+        fr_plan_destroy(plan);
+        return fail(FR_ERR_OUT_OF_MEMORY, "normalised trajectory");
+    }
+    // the whole trajectory's bounds, as one plan would take them
+    if (n) st = fr_normalize_trajectory(d_traj, n, desc->dim, desc->grid_size, tn, nullptr, stream);
+    if (!st && cudaMemsetAsync(d_grid, 0, (size_t)channels * cells * 2 * sizeof(float), s) != cudaSuccess)
+        st = fail(FR_ERR_CUDA, "grid memset");
+    for (size_t b = 0; !st && b < n; b += partition) {
+        const size_t m = std::min(partition, n - b);
+        st = fr_plan_set_trajectory(plan, tn + 4 * b, m, stream);
+        if (!st) st = grid_run(plan, d_kdata + 2 * b, d_dcf + b, channels, d_grid, s, false, n);
+    }
+    if (tn) cudaFreeAsync(tn, s);
+    fr_plan_destroy(plan);
+    return st;
+}
+
 // --------------------------------------------------------------------------
 // Density compensation and degridding
 // --------------------------------------------------------------------------

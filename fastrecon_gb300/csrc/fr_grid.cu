@@ -69,6 +69,9 @@ struct GridParams {
     const float *item_inv = nullptr;    // per work item: inverse fixed-point scale
     int tap_words = 0;
     long long kstride = 0;    // complex values per sample row of the sample-major k-space
+    int *err = nullptr;       // mapped error word
+    int accumulate = 0;       // add the tiles to the grid instead of overwriting it (sample partitions)
+    long long kin_stride = 0; // complex values between coils of the caller's coil-major k-space (0: n)
 };
 
 // Column swizzle of cell i in a row of R floats: keeps (re, im) pairs
@@ -150,6 +153,25 @@ __device__ __forceinline__ void sts_s32x2(unsigned a, int2 v)
     asm volatile("st.shared.v2.s32 [%0], {%1, %2};" ::"r"(a), "r"(v.x), "r"(v.y) : "memory");
 }
 
+// A cell pair / cell of the grid: stored, or added to what is there when the
+// plan accumulates sample partitions into one grid.
+__device__ __forceinline__ void put_cells(float4 *dst, float4 v, int add)
+{
+    if (add) {
+        const float4 o = *dst;
+        v = make_float4(__fadd_rn(o.x, v.x), __fadd_rn(o.y, v.y), __fadd_rn(o.z, v.z), __fadd_rn(o.w, v.w));
+    }
+    *dst = v;
+}
+__device__ __forceinline__ void put_cells(float2 *dst, float2 v, int add)
+{
+    if (add) {
+        const float2 o = *dst;
+        v = make_float2(__fadd_rn(o.x, v.x), __fadd_rn(o.y, v.y));
+    }
+    *dst = v;
+}
+
 // Flush (or zero-fill) the tile's cells for one coil group.  Threads map to
 // (x pair, row): each writes two consecutive x cells as one 16-byte store
 // (even tile x extent and grid size), rows advance without divisions.
@@ -191,7 +213,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
                 const float ir = inv_scale[2 * cl], ii = inv_scale[2 * cl + 1];
                 v = make_float4((float)a.x * ir * sa, (float)a.y * ii * sa, (float)b.x * ir * sb, (float)b.y * ii * sb);
             }
-            gridc[(size_t)(cg * CG + cl) * cstride4] = v;
+            put_cells(&gridc[(size_t)(cg * CG + cl) * cstride4], v, P.accumulate);
         }
         return;
     }
@@ -224,7 +246,7 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
                             }
                         }
                     }
-                    gridc[(((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1] = v;
+                    put_cells(&gridc[(((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1], v, P.accumulate);
                 }
                 ly += dy;
                 lz += dz;
@@ -256,7 +278,8 @@ __device__ __forceinline__ void write_cell_group(const GridParams &P, float *gri
                 v.y = -v.y;
             }
         }
-        grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+        put_cells(&grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx], v,
+                  P.accumulate);
     }
 }
 
@@ -399,8 +422,9 @@ __device__ __forceinline__ void lane_kspace(const GridParams &P, int cg, int f0,
         const int fl = f0 + 32 * k;
         const int coil = cg * CG + (fl >> 1);
         coil_ok[k] = (fl >> 1) < CG && coil < P.channels;
-        kdf[k] = P.kdata + 2 * (size_t)P.channels * (size_t)s_off +
-                 2 * (size_t)(coil_ok[k] ? coil : 0) * (P.sample_major ? (size_t)1 : (size_t)n_f) + (fl & 1);
+        const size_t cstride = P.sample_major ? (size_t)1 : P.frame_off ? (size_t)n_f : (size_t)P.kin_stride;
+        kdf[k] = P.kdata + 2 * (size_t)P.channels * (size_t)s_off + 2 * (size_t)(coil_ok[k] ? coil : 0) * cstride +
+                 (fl & 1);
     }
 }
 
@@ -941,7 +965,8 @@ __global__ void __launch_bounds__(kReduceThreads) reduce_splits_kernel(GridParam
         for (int cl = threadIdx.x / npair; cl < ncl; cl += cstep) {
             const float2 a = *reinterpret_cast<const float2 *>(sum + il * R + ((2 * cl) ^ swa));
             const float2 b = *reinterpret_cast<const float2 *>(sum + (il + 1) * R + ((2 * cl) ^ swb));
-            gridc[(size_t)(cg * CG + cl) * (cells >> 1)] = make_float4(a.x * sa, a.y * sa, b.x * sb, b.y * sb);
+            put_cells(&gridc[(size_t)(cg * CG + cl) * (cells >> 1)], make_float4(a.x * sa, a.y * sa, b.x * sb, b.y * sb),
+                      P.accumulate);
         }
         return;
     }
@@ -956,7 +981,8 @@ __global__ void __launch_bounds__(kReduceThreads) reduce_splits_kernel(GridParam
             v.x = -v.x;
             v.y = -v.y;
         }
-        grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx] = v;
+        put_cells(&grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx], v,
+                  P.accumulate);
     }
 }
 
@@ -988,7 +1014,7 @@ __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const floa
                                                                       const float *__restrict__ dcf,
                                                                       float2 *__restrict__ out,
                                                                       float *__restrict__ mag, long long n,
-                                                                      int channels, int cstride)
+                                                                      int channels, int cstride, long long in_stride)
 {
     extern __shared__ float2 tr[];  // [channels][kTrSamples + 1]
     __shared__ float dsh[kTrSamples];
@@ -1002,7 +1028,7 @@ __global__ void __launch_bounds__(kTrThreads) transpose_kspace_kernel(const floa
         for (int k = 0; k < kTrPer; ++k) {
             const int i = i0 + k * kTrThreads + threadIdx.x;
             const int c = i / kTrSamples, j = i % kTrSamples;
-            v[k] = i < total && j < ns ? in[(size_t)c * n + s0 + j] : make_float2(0.f, 0.f);
+            v[k] = i < total && j < ns ? in[(size_t)c * in_stride + s0 + j] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int k = 0; k < kTrPer; ++k) {
@@ -1135,7 +1161,8 @@ void default_tiling(int dim, int *tile, int *coil_group, int channels)
     }
 }
 
-int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s)
+int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s,
+                   size_t kin_stride)
 {
     p->kt_prepared = nullptr;
     if (p->n == 0) return FR_OK;
@@ -1149,7 +1176,7 @@ int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int chan
                                      (int)trsmem));
     transpose_kspace_kernel<<<(unsigned)((p->n + kTrSamples - 1) / kTrSamples), kTrThreads, trsmem, s>>>(
         reinterpret_cast<const float2 *>(d_kdata), d_dcf, p->kt.as<float2>(), p->kmag.as<float>(), (long long)p->n,
-        channels, cstride);
+        channels, cstride, (long long)(kin_stride ? kin_stride : p->n));
     FR_CHECK_LAUNCH("transpose_kspace_kernel");
     p->kt_prepared = d_kdata;
     p->kt_prepared_channels = channels;
@@ -1157,8 +1184,11 @@ int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int chan
 }
 
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
-             cudaStream_t s, bool skip_empty)
+             cudaStream_t s, bool skip_empty, size_t kin_stride)
 {
+    if (kin_stride && kin_stride < p->n) return fail(FR_ERR_INVALID_ARGUMENT, "coil stride below the samples");
+    const bool accumulate = (p->flags & FR_PLAN_ACCUMULATE) != 0;
+    skip_empty = skip_empty || accumulate;  // adding zeros is a no-op
     if (!p->planned) return fail(FR_ERR_NOT_PLANNED, "fr_grid called before fr_plan_set_trajectory");
     if (channels <= 0) return fail(FR_ERR_INVALID_ARGUMENT, "channels must be positive");
     const int R = floats_per_cell(p->coil_group);
@@ -1195,6 +1225,8 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     P.nwork = 0;
     P.sample_major = 0;
     P.skip_empty = skip_empty ? 1 : 0;
+    P.accumulate = accumulate ? 1 : 0;
+    P.kin_stride = (long long)(kin_stride ? kin_stride : p->n);
     const size_t trsmem = (size_t)channels * (kTrSamples + 1) * sizeof(float2);
     P.mag = nullptr;
     P.kstride = channels;
@@ -1211,7 +1243,7 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
         const bool ready = p->kt_prepared == d_kdata && p->kt_prepared_channels == channels;
         p->kt_prepared = nullptr;
         if (!ready) {
-            const int st = kspace_prepare(p, d_kdata, d_dcf, channels, s);
+            const int st = kspace_prepare(p, d_kdata, d_dcf, channels, s, kin_stride);
             p->kt_prepared = nullptr;
             if (st) return st;
         }
@@ -1325,6 +1357,7 @@ int grid_into(const GridInto &gi, const float *d_kdata, const float *d_dcf, int 
     P.sample_major = 0;
     P.mag = nullptr;
     P.skip_empty = 0;
+    P.kin_stride = (long long)gi.n;
     if (gi.nitems == 0) return FR_OK;
     if (gi.dim == 3) {
         switch (R) {

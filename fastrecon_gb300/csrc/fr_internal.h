@@ -144,13 +144,16 @@ namespace fr {
 int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s);
 // skip_empty: leave the cells of tiles without samples unwritten (the
 // caller's next reader masks them with the plan's tile bitmap).
+// kin_stride: complex values between coils of d_kdata (0: the plan's n),
+// for a sample range of a larger coil-major k-space.
 int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, float *d_grid,
-             cudaStream_t s, bool skip_empty = false);
+             cudaStream_t s, bool skip_empty = false, size_t kin_stride = 0);
 // The scatter's sample-major dcf * k-space copy, made ahead of grid_run
 // (e.g. on another stream while the plan's kernels run); the next grid_run
 // with the same k-space pointer and channel count uses it instead of making
 // its own.  The caller orders that grid_run after this copy.
-int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s);
+int kspace_prepare(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, cudaStream_t s,
+                   size_t kin_stride = 0);
 int sample_ranges_run(fr_plan p, int *d_start, int *d_end, cudaStream_t s);
 // sos_mode: 2 = the whole SoS (sqrt, / deapod); for coils in slabs 0 = store
 // the plain sum of |x|^2, | 1 = add to the sum already in d_out.

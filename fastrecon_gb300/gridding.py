@@ -51,6 +51,22 @@ def grid_size(recon_size: int, overgrid_factor: float) -> int:
     return int(np.float32(recon_size) * np.float32(overgrid_factor))
 
 
+def _plan_desc(dim, grid_size, kernel_width, lut, tile, coil_group, chunk, checkerboard, tap_lists):
+    """fr_plan_desc over ``lut`` (a float32 array the caller keeps alive)."""
+    d = capi.PlanDesc()
+    d.dim = dim
+    d.grid_size = grid_size
+    d.kernel_width = kernel_width
+    d.lut_length = len(lut)
+    d.lut = lut.ctypes.data_as(C.POINTER(C.c_float))
+    for i in range(3):
+        d.tile[i] = int(tile[i]) if i < len(tile) else 0
+    d.coil_group = coil_group
+    d.chunk = chunk
+    d.flags = (capi.FR_PLAN_CHECKERBOARD if checkerboard else 0) | (0 if tap_lists else capi.FR_PLAN_NO_TAP_LISTS)
+    return d
+
+
 class GridPlan:
     """GridLut::plan + execute on the device.
 
@@ -64,17 +80,7 @@ class GridPlan:
         if lut is None:
             lut = kb_lut(kernel_width, overgrid_factor, lut_length)
         self.lut = np.ascontiguousarray(lut, np.float32)
-        d = capi.PlanDesc()
-        d.dim = dim
-        d.grid_size = grid_size
-        d.kernel_width = kernel_width
-        d.lut_length = len(self.lut)
-        d.lut = self.lut.ctypes.data_as(C.POINTER(C.c_float))
-        for i in range(3):
-            d.tile[i] = int(tile[i]) if i < len(tile) else 0
-        d.coil_group = coil_group
-        d.chunk = chunk
-        d.flags = (capi.FR_PLAN_CHECKERBOARD if checkerboard else 0) | (0 if tap_lists else capi.FR_PLAN_NO_TAP_LISTS)
+        d = _plan_desc(dim, grid_size, kernel_width, self.lut, tile, coil_group, chunk, checkerboard, tap_lists)
         h = C.c_void_p()
         check(self.lib.fr_plan_create(C.byref(d), C.byref(h)), "fr_plan_create")
         self.h = h
@@ -200,6 +206,31 @@ class GridPlan:
         w = torch.ones(self.n, dtype=torch.float32, device="cuda") if w0 is None else w0.clone().contiguous()
         check(self.lib.fr_dcf_pipe(self.h, int(iterations), _ptr(w), C.c_void_p(_stream(stream))), "fr_dcf_pipe")
         return w
+
+
+def grid_partitioned(dim: int, grid_size: int, traj, kdata, dcf, partition: int, kernel_width: float = 4.0,
+                     lut=None, lut_length: int = 512, overgrid_factor: float = 2.0, tile=(0, 0, 0),
+                     coil_group: int = 0, chunk: int = 0, checkerboard: bool = False, tap_lists: bool = True,
+                     out=None, stream=None):
+    """cuGridLut's partitioned plan (fr_grid_partitioned): the trajectory
+    normalised once, then planned and gridded ``partition`` samples at a time
+    into one grid.  traj: (N, 4) float32 raw coordinates; kdata: (C, N)
+    complex64; dcf: (N,) float32 -> (C, G^d) complex64."""
+    torch = _torch()
+    lib = capi.load()
+    assert traj.is_cuda and traj.dtype == torch.float32 and traj.shape[-1] == 4
+    assert kdata.dtype == torch.complex64 and kdata.is_cuda and dcf.is_cuda
+    if lut is None:
+        lut = kb_lut(kernel_width, overgrid_factor, lut_length)
+    lut = np.ascontiguousarray(lut, np.float32)
+    d = _plan_desc(dim, grid_size, kernel_width, lut, tile, coil_group, chunk, checkerboard, tap_lists)
+    traj, kdata, dcf = traj.contiguous(), kdata.contiguous(), dcf.contiguous()
+    ch = kdata.shape[0]
+    if out is None:
+        out = torch.empty((ch, grid_size ** dim), dtype=torch.complex64, device="cuda")
+    check(lib.fr_grid_partitioned(C.byref(d), _ptr(traj), traj.shape[0], _ptr(kdata), _ptr(dcf), ch, _ptr(out),
+                                  int(partition), C.c_void_p(_stream(stream))), "fr_grid_partitioned")
+    return out
 
 
 def dcf_analytic(traj, dim: int, power: float = 1.0, stream=None):

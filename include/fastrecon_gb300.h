@@ -87,10 +87,15 @@ enum {
                                        grid units (ReconData::normalizeTraj was
                                        applied, e.g. by fr_normalize_trajectory):
                                        bin it as is */
-    FR_PLAN_NO_TAP_LISTS = 1u << 2  /* keep no per-sample tap lists: the
+    FR_PLAN_NO_TAP_LISTS = 1u << 2, /* keep no per-sample tap lists: the
                                        scatter evaluates each bin record's
                                        kernel taps itself (saves ~170 bytes
                                        per 3D sample of device memory, slower) */
+    FR_PLAN_ACCUMULATE = 1u << 3    /* fr_grid adds the plan's samples to
+                                       d_grid instead of overwriting it (cells
+                                       of tiles without samples are left as
+                                       they are): one grid from several plans
+                                       over sample ranges of one trajectory */
 };
 
 /* ReconData::normalizeTraj (ReconData.cpp:211-225) on the device: component
@@ -174,6 +179,26 @@ long long fr_kernel_launches(void);
  * ---------------------------------------------------------------------- */
 int fr_grid(fr_plan plan, const float *d_kdata, const float *d_dcf, int channels,
             float *d_grid, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Gridding in sample partitions: cuGridLut's partitioned plan
+ * (cuGridLut::setNumOfPartitions, cuGridLut.h:40-42; cuGridLut.cu:128-149,
+ * 182-220), for trajectories whose plan would not fit in device memory.
+ *
+ * Normalises the whole trajectory once (ReconData::normalizeTraj bounds,
+ * ReconData.cpp:211-225, as fr_plan_set_trajectory would), zeroes d_grid,
+ * then plans and grids consecutive ranges of `partition` samples with one
+ * FR_PLAN_PRENORMALIZED | FR_PLAN_ACCUMULATE plan, each range's tiles added
+ * to the grid.  Device memory beyond the caller's buffers: the normalised
+ * trajectory (16 bytes per sample) plus a plan for `partition` samples.
+ * d_kdata: channels x n complex64 (coil-major, as fr_grid); d_grid: channels
+ * x G^d complex64, fully overwritten.  `partition` = 0 or >= n grids in one
+ * plan.  The result equals fr_grid's to float rounding (each range's tile
+ * sums are rounded to float before they are added).  Synchronises `stream`
+ * once per range.
+ * ---------------------------------------------------------------------- */
+int fr_grid_partitioned(const fr_plan_desc *desc, const float *d_traj, size_t n, const float *d_kdata,
+                        const float *d_dcf, int channels, float *d_grid, size_t partition, void *stream);
 
 /* ------------------------------------------------------------------------
  * Gridding without device allocation.  No counterpart in the reference.
