@@ -117,18 +117,65 @@ void cuGridLut<T>::plan(unsigned reconSize, float overGridFactor, float kWidth, 
     d.flags = FR_PLAN_PRENORMALIZED;
     fr_ok(fr_plan_create(&d, &m_plan), "fr_plan_create");
     m_grid_cache.reset();
+    m_kwidth = kWidth;
+    m_partitioned = false;
     const auto &traj = m_cuData.cuGetTraj();
-    fr_ok(fr_plan_set_trajectory(m_plan, reinterpret_cast<const float *>(traj.data()), traj.size(), nullptr),
-          "fr_plan_set_trajectory");
+    const int st = fr_plan_set_trajectory(m_plan, reinterpret_cast<const float *>(traj.data()), traj.size(), nullptr);
+    if (st == FR_ERR_OUT_OF_MEMORY) {
+        // cuGridLut.cu:182-220 partitions its pair map instead; the plan's
+        // partial buffers are released for the partitions' plans
+        fr_plan_destroy(m_plan);
+        m_plan = nullptr;
+        m_partitioned = true;
+    } else {
+        fr_ok(st, "fr_plan_set_trajectory");
+    }
+}
+
+// All channels of the device k-space into d_grid: one plan, or sample
+// partitions when the single plan did not fit.
+template <typename T>
+void cuGridLut<T>::gridAll(float *d_grid)
+{
+    const float *kd = reinterpret_cast<const float *>(m_cuData.cuGetAllChannels());
+    const float *dcf = reinterpret_cast<const float *>(m_cuData.cuGetDcf().data());
+    const int C = m_cuData.channels();
+    m_last_partitions = 0;
+    if (!m_partitioned) {
+        fr_ok(fr_grid(m_plan, kd, dcf, C, d_grid, nullptr), "fr_grid");
+        return;
+    }
+    const std::vector<float> *lut = this->m_kernel->getKernelData();
+    fr_plan_desc d = {};
+    d.dim = (int)this->m_dim;
+    d.grid_size = this->m_gridSize;
+    d.kernel_width = m_kwidth;
+    d.lut_length = (int)lut->size();
+    d.lut = lut->data();
+    for (int i = 0; i < 3; ++i) d.tile[i] = m_tile[i];
+    d.coil_group = m_coil_group;
+    d.flags = FR_PLAN_PRENORMALIZED;
+    const auto &traj = m_cuData.cuGetTraj();
+    const std::size_t n = traj.size();
+    std::size_t parts = (std::size_t)std::max(m_gpu_partitions, 2);
+    for (;;) {
+        const std::size_t part = (n + parts - 1) / parts;
+        const int st = fr_grid_partitioned(&d, reinterpret_cast<const float *>(traj.data()), n, kd, dcf, C, d_grid,
+                                           part, nullptr);
+        if (st == FR_ERR_OUT_OF_MEMORY && part > 1) {
+            parts *= 2;
+            continue;
+        }
+        fr_ok(st, "fr_grid_partitioned");
+        m_last_partitions = (int)((n + part - 1) / std::max<std::size_t>(part, 1));
+        return;
+    }
 }
 
 template <typename T>
 void cuGridLut<T>::executeInto(cuImageData<T> &img)
 {
-    fr_ok(fr_grid(m_plan, reinterpret_cast<const float *>(m_cuData.cuGetAllChannels()),
-                  reinterpret_cast<const float *>(m_cuData.cuGetDcf().data()), m_cuData.channels(),
-                  reinterpret_cast<float *>(img.cuData()), nullptr),
-          "fr_grid");
+    gridAll(reinterpret_cast<float *>(img.cuData()));
     img.cuMarkModified();
 }
 
@@ -144,7 +191,7 @@ void cuGridLut<T>::executeInto(cuImageData<T> &img)
 template <typename T>
 std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
 {
-    if (m_plan == nullptr) {
+    if (m_plan == nullptr && !m_partitioned) {
         std::cerr << "Error: run cuGridLut<T> first.";
         exit(1);
     }
@@ -160,8 +207,9 @@ std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
         executeInto(*img);
         return img;
     }
-    const bool valid = m_grid_cache && m_cache_generation == m_cuData.cuGeneration() && m_cache_channels == C &&
-                       m_cuData.cuDeviceChannelsRaw() != nullptr;
+    // fr_grid_update needs the single plan: partitioned grids regrid in full
+    const bool valid = m_grid_cache && !m_partitioned && m_cache_generation == m_cuData.cuGeneration() &&
+                       m_cache_channels == C && m_cuData.cuDeviceChannelsRaw() != nullptr;
     if (valid) {
         // group the pending readouts by acquisition: one fr_grid_update per
         // updated acquisition, with every channel's row (unchanged rows give
@@ -189,10 +237,7 @@ std::shared_ptr<ImageData<T>> cuGridLut<T>::execute()
         m_last_incremental = true;
     } else {
         m_grid_cache.reset(new cuComplexVector<T>(cells * (std::size_t)C));
-        fr_ok(fr_grid(m_plan, reinterpret_cast<const float *>(m_cuData.cuGetAllChannels()),
-                      reinterpret_cast<const float *>(m_cuData.cuGetDcf().data()), C,
-                      reinterpret_cast<float *>(m_grid_cache->data()), nullptr),
-              "fr_grid");
+        gridAll(reinterpret_cast<float *>(m_grid_cache->data()));
         m_cache_generation = m_cuData.cuGeneration();
         m_cache_channels = C;
     }

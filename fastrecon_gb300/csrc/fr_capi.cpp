@@ -458,24 +458,28 @@ int fr_grid_partitioned(const fr_plan_desc *desc, const float *d_traj, size_t n,
     const size_t cells = desc->dim == 3 ? G * G * G : G * G;
     if (partition == 0 || partition > n) partition = n;
 
+    const bool prenormalized = (desc->flags & FR_PLAN_PRENORMALIZED) != 0;
     fr_plan_desc d = *desc;
     d.flags |= FR_PLAN_PRENORMALIZED | FR_PLAN_ACCUMULATE;
     fr_plan plan = nullptr;
     int st = fr_plan_create(&d, &plan);
     if (st) return st;
     float *tn = nullptr;
-    if (n && cudaMallocAsync(reinterpret_cast<void **>(&tn), n * 4 * sizeof(float), s) != cudaSuccess) {
-        cudaGetLastError();
-        fr_plan_destroy(plan);
-        return fail(FR_ERR_OUT_OF_MEMORY, "normalised trajectory");
+    if (n && !prenormalized) {
+        if (cudaMallocAsync(reinterpret_cast<void **>(&tn), n * 4 * sizeof(float), s) != cudaSuccess) {
+            cudaGetLastError();
+            fr_plan_destroy(plan);
+            return fail(FR_ERR_OUT_OF_MEMORY, "normalised trajectory");
+        }
+        // the whole trajectory's bounds, as one plan would take them
+        st = fr_normalize_trajectory(d_traj, n, desc->dim, desc->grid_size, tn, nullptr, stream);
     }
-    // the whole trajectory's bounds, as one plan would take them
-    if (n) st = fr_normalize_trajectory(d_traj, n, desc->dim, desc->grid_size, tn, nullptr, stream);
+    const float *traj = prenormalized ? d_traj : tn;
     if (!st && cudaMemsetAsync(d_grid, 0, (size_t)channels * cells * 2 * sizeof(float), s) != cudaSuccess)
         st = fail(FR_ERR_CUDA, "grid memset");
     for (size_t b = 0; !st && b < n; b += partition) {
         const size_t m = std::min(partition, n - b);
-        st = fr_plan_set_trajectory(plan, tn + 4 * b, m, stream);
+        st = fr_plan_set_trajectory(plan, traj + 4 * b, m, stream);
         if (!st) st = grid_run(plan, d_kdata + 2 * b, d_dcf + b, channels, d_grid, s, false, n);
     }
     if (tn) cudaFreeAsync(tn, s);

@@ -3,8 +3,11 @@
 //
 // Differences from the reference: the plan belongs to this object and is
 // built for this object's trajectory (the reference caches one plan per
-// process, keyed on nothing, cuGridLut.cu:14-18,158-159); there are no host-side
-// partitions, so setNumOfPartitions only records the value.
+// process, keyed on nothing, cuGridLut.cu:14-18,158-159).  Partitions
+// (setNumOfPartitions) are used only when the single plan does not fit in
+// device memory: execute() then grids sample ranges with
+// fr_grid_partitioned (at least 2 partitions, doubled while a partition's
+// plan still does not fit) instead of chunking a host-side pair map.
 #ifndef FASTRECON_CUGRIDLUT_H
 #define FASTRECON_CUGRIDLUT_H
 
@@ -32,11 +35,18 @@ public:
     // since the one before (ReconData::updateSingleAcquisition) instead of
     // the whole k-space.
     bool lastExecuteIncremental() const { return m_last_incremental; }
+    // Sample partitions of the last execute() (0: one plan).
+    int lastExecutePartitions() const { return m_last_partitions; }
 
 private:
     cuReconData<T> &m_cuData;
     fr_plan_s *m_plan = nullptr;
     int m_gpu_partitions = 1;
+    // the single plan did not fit: grid in sample partitions
+    bool m_partitioned = false;
+    int m_last_partitions = 0;
+    float m_kwidth = 0.f;
+    void gridAll(float *d_grid);
     int m_tile[3] = {0, 0, 0};
     int m_coil_group = 0;
     // streaming acquisitions: the grid of the last execute(), kept once the

@@ -186,7 +186,8 @@ int fr_grid(fr_plan plan, const float *d_kdata, const float *d_dcf, int channels
  * 182-220), for trajectories whose plan would not fit in device memory.
  *
  * Normalises the whole trajectory once (ReconData::normalizeTraj bounds,
- * ReconData.cpp:211-225, as fr_plan_set_trajectory would), zeroes d_grid,
+ * ReconData.cpp:211-225, as fr_plan_set_trajectory would; skipped when
+ * desc->flags holds FR_PLAN_PRENORMALIZED), zeroes d_grid,
  * then plans and grids consecutive ranges of `partition` samples with one
  * FR_PLAN_PRENORMALIZED | FR_PLAN_ACCUMULATE plan, each range's tiles added
  * to the grid.  Device memory beyond the caller's buffers: the normalised

@@ -10,7 +10,8 @@
 // channel, upd_acq.i32 (NUPD acquisition indices) and upd_k_c.c64 (the new
 // readout k of channel c).  Writes grid0.c64, grid1.c64, grid2.c64 (all
 // channels: before the updates, after the first half, after the rest),
-// traj_norm.f32 and dcf.f32 (after plan), and prints incremental1=0|1 and
+// traj_norm.f32 and dcf.f32 (after plan), and prints partitions=P (sample
+// partitions of the first execute, 0: one plan), incremental1=0|1 and
 // incremental2=0|1 for the two executes after updates.
 #include <cstdio>
 #include <cstdlib>
@@ -79,12 +80,13 @@ int main(int argc, char **argv)
     grid->plan(recon, os, width, klength);
     auto img0 = grid->execute();
     write_grid(dir + "/grid0.c64", *img0);
+    auto *cugrid = dynamic_cast<cuGridLut<float> *>(grid.get());
+    std::cout << "partitions=" << cugrid->lastExecutePartitions() << std::endl;
 
     // two rounds of updates (the first half of the list, then the rest): the
     // first execute after updates regrids everything and keeps the grid, the
     // second regrids only the updated readouts
     auto acqs = read_file<std::vector<int>>(dir + "/upd_acq.i32", nupd);
-    auto *cugrid = dynamic_cast<cuGridLut<float> *>(grid.get());
     for (int round = 0; round < 2; ++round) {
         const int k0 = round == 0 ? 0 : nupd / 2, k1 = round == 0 ? nupd / 2 : nupd;
         for (int k = k0; k < k1; ++k)

@@ -103,15 +103,9 @@ def test_cpp_stream_main_builds(tmp_path):
     assert os.path.exists(compile_stream(str(tmp_path)))
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small"])
-def test_cpp_streaming_acquisitions_vs_oracle(tmp_path, oracle, name):
-    """ReconData::loadTraj (interleaved trajectory + DCF) and
-    updateSingleAcquisition through the C++ API: the trajectory after plan is
-    the reference's bit for bit, and the grids before the updates, after a
-    first round (full regrid) and after a second round (only the updated
-    readouts regridded, fr_grid_update) equal the oracle's grid of the same
-    k-space at 1e-5."""
+def _run_stream(tmp_path, oracle, name, env=None):
+    """Runs stream_main on a golden case and checks its trajectory, DCF and
+    three grids against the oracle; returns its stdout."""
     c = load_case(name)
     d = str(tmp_path)
     exe = compile_stream(d)
@@ -130,9 +124,9 @@ def test_cpp_streaming_acquisitions_vs_oracle(tmp_path, oracle, name):
             new[k, ch].tofile(os.path.join(d, f"upd_{k}_{ch}.c64"))
     args = [exe, d, str(S), str(A), str(C), str(dim), str(c["recon"]), repr(c["os"]), repr(c["W"]), str(c["L"]),
             str(len(acqs))]
-    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300,
+                       env=None if env is None else {**os.environ, **env})
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "incremental1=0" in r.stdout and "incremental2=1" in r.stdout, r.stdout
     tn = np.fromfile(os.path.join(d, "traj_norm.f32"), np.float32).reshape(-1, 4)
     assert np.array_equal(tn.view(np.uint32), c["traj_norm"].view(np.uint32))
     assert np.array_equal(np.fromfile(os.path.join(d, "dcf.f32"), np.float32), c["dcf"])
@@ -147,3 +141,34 @@ def test_cpp_streaming_acquisitions_vs_oracle(tmp_path, oracle, name):
         err = rel_l2(got, want)
         print(f"{name} {g_name}: rel-L2 vs oracle {err:.2e}")
         assert err <= 1e-5, g_name
+    return r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small"])
+def test_cpp_streaming_acquisitions_vs_oracle(tmp_path, oracle, name):
+    """ReconData::loadTraj (interleaved trajectory + DCF) and
+    updateSingleAcquisition through the C++ API: the trajectory after plan is
+    the reference's bit for bit, and the grids before the updates, after a
+    first round (full regrid) and after a second round (only the updated
+    readouts regridded, fr_grid_update) equal the oracle's grid of the same
+    k-space at 1e-5."""
+    out = _run_stream(tmp_path, oracle, name)
+    assert "partitions=0" in out and "incremental1=0" in out and "incremental2=1" in out, out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radial2d_small", "koosh3d_small"])
+def test_cpp_partitions_when_the_plan_does_not_fit(tmp_path, oracle, name):
+    """cuGridLut with a plan that does not fit in device memory (host-side
+    fault injection: reservations of 16 bytes per sample -- the plan's
+    trajectory copy -- or more fail as cudaMalloc would) grids in sample
+    partitions (fr_grid_partitioned), as the reference partitions its pair
+    map (cuGridLut.cu:182-220), doubling the partitions while a partition's
+    plan (its split-tile partials included) still does not fit; every
+    execute regrids in full, and the grids equal the oracle's."""
+    n = load_case(name)["traj"].shape[0]
+    out = _run_stream(tmp_path, oracle, name, env={"FR_FAIL_ALLOC_BYTES": str(16 * n)})
+    parts = int(out.split("partitions=")[1].split()[0])
+    assert parts >= 2, out
+    assert "incremental1=0" in out and "incremental2=0" in out, out

@@ -122,9 +122,14 @@ def test_out_of_memory_paths_with_injected_failures(torch):
     from fastrecon_gb300.capi import FastreconError
     c = load_case("koosh3d_small")
     n = c["traj"].shape[0]
+    # one work item per tile (no split-tile partials): the tap slots are the
+    # plan's largest reservation
+    p0, _ = _grid(torch, c, c["kdata"], chunk=16384)
+    words = p0.tap_words()
+    assert words > 0 and p0.stats()["slots"] == 0
     try:
-        os.environ["FR_FAIL_ALLOC_BYTES"] = str(n * 30 * 4)  # below the tap slots, above everything else
-        p, g = _grid(torch, c, c["kdata"])
+        os.environ["FR_FAIL_ALLOC_BYTES"] = str(n * words * 4)  # the tap slots and nothing else
+        p, g = _grid(torch, c, c["kdata"], chunk=16384)
         assert p.tap_words() == 0
         assert rel_l2(g, c["grid"]) <= TOL
         os.environ["FR_FAIL_ALLOC_BYTES"] = str(n * 8)  # below the trajectory copy
