@@ -381,6 +381,7 @@ def run_ours(args, w):
     elapsed = e0.elapsed_time(e1)  # ms
     scatter_ms, scatter_n = rec.profile_read()
     rec.profile(False)
+    taps = rec.tap_words() > 0
     from fastrecon_gb300 import replicas
     elapsed = replicas.max_over_ranks(elapsed, dist, device=dev)  # replicas: the slowest rank's time
     ms = elapsed / args.steps
@@ -454,7 +455,8 @@ def run_ours(args, w):
     per_launch_ms = scatter_ms / max(scatter_n, 1)
     achieved = algo / (per_launch_ms / 1e3) / 1e9
     traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "grid_tiles_traffic.txt")
+    kernel = "grid_taps_kernel" if taps else "grid_tiles_kernel"
+    tr_path = os.path.join(ROOT, "profiles", kernel.replace("_kernel", "") + "_traffic.txt")
     if os.path.exists(tr_path):
         for line in open(tr_path):
             if line.startswith(args.workload + " "):
@@ -470,7 +472,9 @@ def run_ours(args, w):
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "recon_ms": ms,
         "stage_ms": stage_ms,
-        "roofline": {"bound": "hbm", "kernel": "grid_tiles_kernel (KB scatter)", "achieved": achieved,
+        "roofline": {"bound": "hbm",
+                     "kernel": kernel + (" (KB scatter from the plan's tap lists)" if taps else " (KB scatter)"),
+                     "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": algo, "kernel_ms": per_launch_ms, "launches": scatter_n,
                      "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"

@@ -420,6 +420,12 @@ class Recon:
         check(self.lib.fr_recon_plan(self.h, C.byref(h)), "fr_recon_plan")
         return h
 
+    def tap_words(self) -> int:
+        """4-byte tap-list words per sample of the recon's plan (0: the scatter evaluates the taps)."""
+        q = C.c_int()
+        check(self.lib.fr_plan_tap_words(self._plan(), C.byref(q)), "fr_plan_tap_words")
+        return q.value
+
     def profile(self, enable: bool = True):
         """Record CUDA events around the tile scatter kernel of every run."""
         check(self.lib.fr_plan_profile(self._plan(), 1 if enable else 0), "fr_plan_profile")
