@@ -120,6 +120,40 @@ def build_dataset(dim, n_traj, seed, per_traj=20000, residual=False):
     return torch.cat(X), torch.cat(Y), torch.cat(C)
 
 
+def summarise(ev):
+    """Median and 10/90th percentiles of each NRMSE column, per family and overall."""
+    out = {}
+    fams = sorted({e["family"] for e in ev})
+    for key in ("nrmse_learned", "nrmse_learned_refined", "nrmse_plain"):
+        v = np.array([e[key] for e in ev])
+        out[key] = dict(median=float(np.median(v)), p10=float(np.percentile(v, 10)), p90=float(np.percentile(v, 90)),
+                        below_1pct=int((v <= 0.01).sum()))
+        for f in fams:
+            vf = np.array([e[key] for e in ev if e["family"] == f])
+            out[key][f] = dict(n=int(vf.size), median=float(np.median(vf)))
+    out["learned_beats_plain"] = int(sum(e["nrmse_learned"] < e["nrmse_plain"] for e in ev))
+    out["trajectories"] = len(ev)
+    return out
+
+
+def eval_saved(a):
+    """Held-out evaluation of the saved network (the draw continues the
+    training run's held-out sequence: its first trajectories are the ones the
+    training report used)."""
+    path = a.out or model_path(a.dim)
+    net = ld.DCFNet.load(path)
+    rng = np.random.default_rng(a.seed + 12345)
+    held = [draw_trajectory(a.dim, rng, n_max=a.max_samples) for _ in range(a.held_out)]
+    ev = evaluate(net, a.dim, held)
+    rep_path = os.path.splitext(path)[0] + ".json"
+    rep = json.load(open(rep_path)) if os.path.exists(rep_path) else {}
+    rep["held_out_eval"] = dict(trajectories=len(ev), summary=summarise(ev), cases=ev)
+    with open(rep_path, "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps(rep["held_out_eval"]["summary"]))
+    return rep
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--dim", type=int, default=2, choices=(2, 3))
@@ -133,8 +167,12 @@ def main(argv=None):
     ap.add_argument("--out", default=None)
     ap.add_argument("--residual", action="store_true",
                     help="train on log-DCF + log density (radius 2): nearly density-independent targets")
+    ap.add_argument("--eval-only", action="store_true",
+                    help="evaluate the saved model on --held-out trajectories and add the result to its report")
     a = ap.parse_args(argv)
     torch = G_._torch()
+    if a.eval_only:
+        return eval_saved(a)
     t0 = time.time()
     X, Y, Cw = build_dataset(a.dim, a.trajectories, a.seed, residual=a.residual)
     torch.cuda.synchronize()
