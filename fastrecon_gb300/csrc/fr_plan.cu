@@ -367,6 +367,7 @@ struct TapGeom {
     const float4 *lut_e;             // {thr[k+1], lut[k], lut[k+1], 0}
     float smax, kc;
     int L, words;                    // tap words per sample slot
+    int recmax;                      // records (tiles) one sample's range can touch
     int *err;                        // set when a slot would overflow (never, by the slot bound)
 };
 
@@ -455,13 +456,13 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
                                                                  unsigned long long *__restrict__ recs)
 {
     // [kFillThreads][S] slot words (S = words | 1: odd, no bank conflicts),
-    // then the tap counts and the run offsets, kFillRecMax x kFillThreads each
+    // then the tap counts and the run offsets, recmax x kFillThreads each
     extern __shared__ unsigned stage[];
     const int S = tg.words | 1;
     const int lane = threadIdx.x & 31;
     unsigned *mine = stage + threadIdx.x * S;
     unsigned char *cnt = reinterpret_cast<unsigned char *>(stage + kFillThreads * S) + threadIdx.x;
-    unsigned char *off = cnt + kFillRecMax * kFillThreads;
+    unsigned char *off = cnt + tg.recmax * kFillThreads;
     for (size_t base = blockIdx.x * (size_t)kFillThreads; base < n; base += (size_t)gridDim.x * kFillThreads) {
         size_t i = base + threadIdx.x;
         TileWalk w;
@@ -834,13 +835,14 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         return FR_ERR_OUT_OF_MEMORY;
     // tap lists, when the tile and kernel allow them and the memory is there
     p->tap_words = 0;
+    int recmax = 1;
     if (p->taps_enabled && n > 0 && p->err_dev && p->L < (1 << (32 - kTapCellBits)) &&
         (long long)p->tile[0] * p->tile[1] * p->tile[2] <= (1 << kTapCellBits)) {
         if (p->tap_layout_words == 0) tap_slot_layout(p->dim, p->hw, &p->tap_layout_words);
         const int words = p->tap_layout_words;
         // tiles one sample's cell range (at most floor(2 hw) + 1 cells per axis) can touch
         const int F = (int)std::floor(2.0 * p->hw) + 1;
-        int recmax = 1;
+        recmax = 1;
         for (int d = 0; d < p->dim; ++d) recmax *= (F - 1 + p->tile[d] - 1) / p->tile[d] + 1;
         if (words <= kTapRecMax && recmax <= kFillRecMax && F <= 9 && !p->taps.reserve(n * (size_t)words * 4) &&
             !p->trecs.reserve(std::max<long long>(tot.pairs, 1) * 8))
@@ -856,7 +858,10 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         tg.L = p->L;
         tg.words = p->tap_words;
         tg.err = p->err_dev;
-        const size_t smem = (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * kFillRecMax);
+        tg.recmax = recmax;
+        // slot staging plus 2 bytes per possible record: 4 CTAs of 256 per SM
+        // for the 3D 4-wide kernel (42 words, 8 records)
+        const size_t smem = (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * recmax);
         // cells of a sample's range along x: at most floor(2 hw) + 1; the
         // mask walk when a range touches at most 2 tiles per axis and its
         // taps fit one 64-bit mask
