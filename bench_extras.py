@@ -29,6 +29,21 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 
 
+def _roofline(algo_bytes, ms, what):
+    """Achieved HBM bandwidth of `algo_bytes` (the gridding formula N(4d+4) +
+    N C 8 + C G^d 8, summed over frames) in `ms`, against the measured copy
+    bandwidth."""
+    import json
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "measured hbm_gbs (MEASURED_PEAKS.json)"
+    except Exception:
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    achieved = algo_bytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": what, "algorithmic_bytes": int(algo_bytes), "ms": ms, "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src}
+
+
 def _ms(torch, fn, steps, warmup, stream):
     for _ in range(warmup):
         fn()
@@ -74,6 +89,8 @@ def batched_spiral(torch, steps=20, warmup=3, frames=64, coils=12, recon=192, os
             "autotune": {"tile": [d.tile[0], d.tile[1]], "chunk": d.chunk, "coil_group": d.coil_group,
                          "best_ms": tune_ms, "seconds": round(tune_s, 2)},
             "graph_replays_per_batch": launches,
+            "roofline": _roofline(n * (4 * 2 + 4) + n * coils * 8 + frames * coils * G * G * 8, ms,
+                                  "grid_persistent_kernel + split reduction (the replayed graph, all frames)"),
             "workload": f"2D dynamic spiral: {frames} frames x 4-24 variable-density interleaves x {samples} "
                         f"samples (seeded), {coils} coils, {recon}^2 matrix, os {os_} -> {G}^2 grid; one "
                         "persistent launch per batch, replayed from a CUDA graph; tiling from the autotuner"}
@@ -92,7 +109,17 @@ def radial2d(torch, steps=50, warmup=5):
     img = torch.empty(256 * 256, dtype=torch.float32, device="cuda")
     s = torch.cuda.current_stream()
     ms = _ms(torch, lambda: rec.run(traj, dcf, kd, out=img), steps, warmup, s)
+    rec.profile(True)
+    rec.profile_read()
+    for _ in range(steps):
+        rec.run(traj, dcf, kd, out=img)
+    scatter_ms, launches = rec.profile_read()
+    rec.profile(False)
+    G = 512
+    kern = "grid_taps_kernel" if rec.tap_words() > 0 else "grid_tiles_kernel"
     return {"value": n * c / (ms / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_step": ms, "samples": n, "coils": c,
+            "roofline": _roofline(n * (4 * 2 + 4) + n * c * 8 + c * G * G * 8, scatter_ms / max(launches, 1),
+                                  kern + " (one launch per step, CUDA events)"),
             "workload": "2D radial: 256 uniformly spaced spokes x 512 samples, 8 coils, |k| DCF, KB width 4, "
                         "os 2 -> 512^2 grid, 256^2 SoS (plan + grid + FFT + SoS per step)"}
 

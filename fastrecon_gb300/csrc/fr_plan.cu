@@ -482,13 +482,27 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
         // taps per record, then each record's first word, then the taps
         int tot = 0;
         for (int j = 0; j < cnt_t; ++j) cnt[j * kFillThreads] = 0;
-        if (cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, false, cnt, off, mine);
+        // ranges of XR - 1 cells along x (all but samples on a cell
+        // boundary: hw = 2 gives 4 cells unless c - 2 is an integer) walk
+        // one candidate fewer per row
+        const bool narrow = e[0] - s[0] + 1 < XR;
+        if (cnt_t > 0) {
+            if (narrow)
+                sample_taps<XR - 1>(g, tg, c, s, e, w, false, cnt, off, mine);
+            else
+                sample_taps<XR>(g, tg, c, s, e, w, false, cnt, off, mine);
+        }
         for (int j = 0; j < cnt_t; ++j) {
             off[j * kFillThreads] = (unsigned char)min(tot, 255);
             tot += cnt[j * kFillThreads];
             cnt[j * kFillThreads] = 0;
         }
-        if (tot <= tg.words && cnt_t > 0) sample_taps<XR>(g, tg, c, s, e, w, true, cnt, off, mine);
+        if (tot <= tg.words && cnt_t > 0) {
+            if (narrow)
+                sample_taps<XR - 1>(g, tg, c, s, e, w, true, cnt, off, mine);
+            else
+                sample_taps<XR>(g, tg, c, s, e, w, true, cnt, off, mine);
+        }
         if (tot > tg.words) *tg.err = FR_ERR_CAPACITY;  // never: the slot bounds every sample's taps
 
         const int stripe = stripe_of(base + threadIdx.x - lane);
