@@ -16,9 +16,11 @@ LIB_PATH = os.path.join(_PKG, "_lib", "libfastrecon_gb300.so")
 FR_PLAN_CHECKERBOARD = 1
 FR_PLAN_NO_TAP_LISTS = 4
 FR_PLAN_ACCUMULATE = 8
+FR_PLAN_DETERMINISTIC = 16
 FR_RECON_DEAPODIZE = 1
 FR_RECON_CUFFT = 2
 FR_RECON_PRUNED_FFT = 4
+FR_RECON_DETERMINISTIC = 8
 
 _lib = None
 

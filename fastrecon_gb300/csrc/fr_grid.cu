@@ -684,8 +684,8 @@ constexpr int kTapDepth = 4;   // records in flight per warp
 constexpr int kTapList = 64;   // list entries per warp (records hold <= kTapRecMax taps, padded)
 
 // Shared-memory layout of grid_taps_kernel, from its 128-byte aligned base:
-// tile [K][R] int32 | inverse scales [R] (256 B) | weights [L] | per warp a
-// list [kTapList] {address, weight}.
+// tile [K][R] int32 | inverse scales [R] (256 B) | weights [L] | per warp two
+// lists [kTapList] {address, weight} (consecutive records alternate).
 struct TapSmem {
     unsigned inv, lutw, lists, end;
 };
@@ -695,7 +695,7 @@ __host__ __device__ __forceinline__ TapSmem tap_smem_layout(long long K, int R, 
     m.inv = (unsigned)(K * R * 4);
     m.lutw = m.inv + 256u;
     m.lists = m.lutw + (unsigned)((L * 4 + 15) & ~15);
-    m.end = m.lists + (unsigned)(kWarps * kTapList * 8);
+    m.end = m.lists + (unsigned)(kWarps * 2 * kTapList * 8);
     return m;
 }
 
@@ -733,7 +733,7 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
     }
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const unsigned list = acc + L_.lists + (unsigned)(warp * kTapList * 8);
+    const unsigned lists = acc + L_.lists + (unsigned)(warp * 2 * kTapList * 8);
 
     for (int i = threadIdx.x; i < K * R / 4; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutw_s[i] = P.lutw[i];
@@ -788,14 +788,22 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 #pragma unroll
     for (int d = 0; d < kTapDepth; ++d) fetch(cur, d, st[d]);
 
+    static_assert(kTapDepth % 2 == 0 && 32 % kTapDepth == 0, "records alternate lists; batches hold whole groups");
     for (int k0 = 0; k0 < nrec; k0 += kTapDepth) {
         if (k0 > 0 && (k0 & 31) == 0) {
             cur = nxt;
             nxt = load_batch((k0 >> 5) + 1);
         }
+        // the refills of this group come from the next batch only in the
+        // batch's last group
+        const Batch &src = (k0 & 31) == 32 - kTapDepth ? nxt : cur;
 #pragma unroll
         for (int d = 0; d < kTapDepth; ++d) {
             const int k = k0 + d;
+            // consecutive records alternate lists: record k + 1's decode
+            // never overwrites the list record k is still adding from, so
+            // one warp barrier per record (after the decode) orders both
+            const unsigned list = lists + (unsigned)((d & 1) * kTapList * 8);
             const int ntap = st[d].nt;
             const int np = (ntap + PAD - 1) / PAD * PAD;
             const float vs = __fmul_rn(st[d].v, sc);
@@ -823,7 +831,7 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
             // refill this stage with record k + kTapDepth
             const int k2 = k + kTapDepth;
             if (k2 < nrec) {
-                fetch((k2 >> 5) == (k0 >> 5) ? cur : nxt, k2 & 31, st[d]);
+                fetch(src, k2 & 31, st[d]);
             } else {
                 st[d].nt = 0;
             }
@@ -842,7 +850,6 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
                     }
                 }
             }
-            __syncwarp();
         }
     }
     __syncthreads();
@@ -860,7 +867,10 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 
 // Per work item, from the per-sample bounds (mag[s] >= every |dcf * k| of
 // sample s), one warp per item: the sum and the maximum over the item's
-// records with taps.
+// records with taps.  The sum is exact and independent of the records'
+// order: each bound is rounded up to a multiple of 2^-e (2^e bmax = 2^40..41)
+// and the multiples are added as 64-bit integers; the float result is
+// rounded up.
 __global__ void item_bound_kernel(const WorkItem *__restrict__ items, long long nitems,
                                   const unsigned long long *__restrict__ trecs, const float *__restrict__ mag,
                                   float2 *__restrict__ bound)
@@ -869,19 +879,23 @@ __global__ void item_bound_kernel(const WorkItem *__restrict__ items, long long 
     const int lane = threadIdx.x & 31;
     if (w >= nitems) return;
     const WorkItem it = items[w];
-    float bs = 0.f, bm = 0.f;
+    float bm = 0.f;
     for (int j = lane; j < it.count; j += 32) {
         const unsigned long long rw = trecs[it.begin + j];
-        if ((rw >> 40) & 0xFF) {
-            const float a = mag[(unsigned)rw];
-            bs += a;
-            bm = fmaxf(bm, a);
-        }
+        if ((rw >> 40) & 0xFF) bm = fmaxf(bm, mag[(unsigned)rw]);
     }
+    bm = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(bm)));  // bounds are >= 0
+    float bs = 0.f;
+    if (bm > 0.f) {
+        const int e = 40 - ilogbf(bm);
+        unsigned long long q = 0;
+        for (int j = lane; j < it.count; j += 32) {
+            const unsigned long long rw = trecs[it.begin + j];
+            if ((rw >> 40) & 0xFF) q += __float2ull_ru(ldexpf(mag[(unsigned)rw], e));
+        }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        bs += __shfl_xor_sync(0xffffffffu, bs, o);
-        bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+        bs = ldexpf(__ull2float_ru(q), -e);
     }
     if (lane == 0) bound[w] = make_float2(bs, bm);
 }

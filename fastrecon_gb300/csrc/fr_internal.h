@@ -57,6 +57,14 @@ struct SplitTile {
     int pad;
 };
 
+// One bucket of a split tile's records being put in sample order
+// (deterministic plans).
+struct SortBucket {
+    long long start;  // first record
+    int count;
+    int pad;
+};
+
 // Scan tuple over tiles: pairs, work items of occupied tiles, partial
 // slots, split tiles, empty tiles (whose zero-fill items follow every
 // occupied tile's items in the item list).
@@ -129,6 +137,8 @@ struct fr_plan_s {
     fr::DevBuf taps;           // n x tap_words words
     fr::DevBuf trecs;          // npairs words, in bin order: sample | first word << 32 | taps << 40
     fr::DevBuf item_inv;       // per work item: inverse fixed-point scale, then the items' bounds
+    fr::DevBuf sort_tmp;       // deterministic plans: split tiles' records (and tap records) being sorted
+    fr::DevBuf sort_buckets;   // deterministic plans: SortBucket table + its count
     int *err_host = nullptr;   // mapped pinned word the kernels set on an internal error
     int *err_dev = nullptr;
 

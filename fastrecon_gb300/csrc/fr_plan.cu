@@ -722,6 +722,115 @@ __global__ void items_kernel(const int *__restrict__ cnt, const TileScan *__rest
     }
 }
 
+// Deterministic plans (FR_PLAN_DETERMINISTIC).  The bin fill places a
+// tile's records with atomics, so which records each work item of a split
+// tile holds -- and with them each item's fixed-point scale and rounding --
+// varies from run to run.  These two kernels put the records of every split
+// tile in sample order (sample indices are unique within a tile), moving the
+// tap records beside them: the records are bucketed by sample index (one
+// CTA per split tile, buckets of ~kSortBucket records over the tile's
+// index range), then each bucket is rank-sorted by one warp.
+constexpr int kSortBucket = 256;
+constexpr int kSortMaxBuckets = 8192;
+constexpr int kSortThreads = 1024;
+
+__global__ void __launch_bounds__(kSortThreads) split_bucket_kernel(
+    const SplitTile *__restrict__ splits, const TileScan *__restrict__ scan, const int *__restrict__ tile_count,
+    const unsigned long long *__restrict__ recs, const unsigned long long *__restrict__ trecs,
+    unsigned long long *__restrict__ recs_tmp, unsigned long long *__restrict__ trecs_tmp,
+    SortBucket *__restrict__ buckets, int *__restrict__ nbuckets)
+{
+    __shared__ unsigned hist[kSortMaxBuckets];
+    __shared__ unsigned part[kSortThreads / 32];
+    __shared__ unsigned mnmx[2];
+    __shared__ int base;
+    const int t = splits[blockIdx.x].tile;
+    const long long b = scan[t].pairs;
+    const int c = tile_count[t];
+    const int B = min((c + kSortBucket - 1) / kSortBucket, kSortMaxBuckets);
+    if (threadIdx.x == 0) {
+        mnmx[0] = 0xffffffffu;
+        mnmx[1] = 0u;
+        base = atomicAdd(nbuckets, B);
+    }
+    for (int i = threadIdx.x; i < kSortMaxBuckets; i += kSortThreads) hist[i] = 0u;
+    __syncthreads();
+    unsigned lmn = 0xffffffffu, lmx = 0u;
+    for (int i = threadIdx.x; i < c; i += kSortThreads) {
+        const unsigned k = (unsigned)recs[b + i];
+        lmn = min(lmn, k);
+        lmx = max(lmx, k);
+    }
+    lmn = __reduce_min_sync(0xffffffffu, lmn);
+    lmx = __reduce_max_sync(0xffffffffu, lmx);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mnmx[0], lmn);
+        atomicMax(&mnmx[1], lmx);
+    }
+    __syncthreads();
+    const unsigned mn = mnmx[0];
+    const unsigned long long span = (unsigned long long)(mnmx[1] - mn) + 1ull;
+    auto bucket_of = [&](unsigned k) { return (int)(((unsigned long long)(k - mn) * (unsigned)B) / span); };
+    for (int i = threadIdx.x; i < c; i += kSortThreads) atomicAdd(&hist[bucket_of((unsigned)recs[b + i])], 1u);
+    __syncthreads();
+    // exclusive scan of hist[0, kSortMaxBuckets): 8 consecutive entries per thread
+    constexpr int PER = kSortMaxBuckets / kSortThreads;
+    unsigned v[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        v[k] = hist[threadIdx.x * PER + k];
+        sum += v[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned inc = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) part[warp] = inc;
+    __syncthreads();
+    unsigned wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += part[w];
+    unsigned off = wpre + inc - sum;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int i = threadIdx.x * PER + k;
+        if (i < B) buckets[base + i] = SortBucket{b + off, (int)v[k], 0};
+        hist[i] = off;  // cursor
+        off += v[k];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < c; i += kSortThreads) {
+        const unsigned long long r = recs[b + i];
+        const unsigned pos = atomicAdd(&hist[bucket_of((unsigned)r)], 1u);
+        recs_tmp[b + pos] = r;
+        if (trecs) trecs_tmp[b + pos] = trecs[b + i];
+    }
+}
+
+__global__ void split_sort_kernel(const SortBucket *__restrict__ buckets, const int *__restrict__ nbuckets,
+                                  const unsigned long long *__restrict__ recs_tmp,
+                                  const unsigned long long *__restrict__ trecs_tmp,
+                                  unsigned long long *__restrict__ recs, unsigned long long *__restrict__ trecs)
+{
+    const int lane = threadIdx.x & 31;
+    const int nb = *nbuckets;
+    for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < nb;
+         w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const SortBucket bk = buckets[w];
+        const unsigned long long *src = recs_tmp + bk.start;
+        for (int i = lane; i < bk.count; i += 32) {
+            const unsigned long long r = src[i];
+            const unsigned key = (unsigned)r;
+            int rank = 0;
+            for (int j = 0; j < bk.count; ++j) rank += (unsigned)__ldg(src + j) < key ? 1 : 0;
+            recs[bk.start + rank] = r;
+            if (trecs) trecs[bk.start + rank] = trecs_tmp[bk.start + i];
+        }
+    }
+}
+
 // Bit t of the occupancy bitmap: tile t holds at least one bin record.
 __global__ void tile_mask_kernel(const int *__restrict__ cnt, long long ntiles, unsigned *__restrict__ mask)
 {
@@ -896,6 +1005,26 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
                                                              p->chunk, p->items.as<WorkItem>(),
                                                              p->splits.as<SplitTile>());
     FR_CHECK_LAUNCH("items_kernel");
+    if ((p->flags & FR_PLAN_DETERMINISTIC) && p->nsplits > 0) {
+        // split tiles' records in sample order (see split_bucket_kernel)
+        const bool taps = p->tap_words > 0;
+        const long long nb_max = p->npairs / kSortBucket + p->nsplits + 1;
+        if (p->nsplits > INT_MAX || p->sort_tmp.reserve((size_t)p->npairs * 8 * (taps ? 2 : 1)) ||
+            p->sort_buckets.reserve((size_t)nb_max * sizeof(SortBucket) + 16))
+            return FR_ERR_OUT_OF_MEMORY;
+        unsigned long long *rt = p->sort_tmp.as<unsigned long long>();
+        unsigned long long *tt = taps ? rt + p->npairs : nullptr;
+        SortBucket *bk = p->sort_buckets.as<SortBucket>();
+        int *nbk = reinterpret_cast<int *>(bk + nb_max);
+        FR_CUDA(cudaMemsetAsync(nbk, 0, sizeof(int), s));
+        split_bucket_kernel<<<(unsigned)p->nsplits, kSortThreads, 0, s>>>(
+            p->splits.as<SplitTile>(), scan, p->tile_count.as<int>(), p->pairs.as<unsigned long long>(),
+            taps ? p->trecs.as<unsigned long long>() : nullptr, rt, tt, bk, nbk);
+        FR_CHECK_LAUNCH("split_bucket_kernel");
+        split_sort_kernel<<<152 * 8, 256, 0, s>>>(bk, nbk, rt, tt, p->pairs.as<unsigned long long>(),
+                                                 taps ? p->trecs.as<unsigned long long>() : nullptr);
+        FR_CHECK_LAUNCH("split_sort_kernel");
+    }
     if (p->tile_mask.reserve((size_t)((p->ntiles + 31) / 32) * 4)) return FR_ERR_OUT_OF_MEMORY;
     tile_mask_kernel<<<grid_blocks((p->ntiles + 31) / 32, 256), 256, 0, s>>>(p->tile_count.as<int>(), p->ntiles,
                                                                               p->tile_mask.as<unsigned>());

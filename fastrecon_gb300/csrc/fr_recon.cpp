@@ -120,7 +120,8 @@ int fr_recon_create(const fr_recon_desc *d, fr_recon *out)
         while (cg < d->channels && cg < 16) cg <<= 1;
         pd.coil_group = cg;
     }
-    pd.flags = r->checkerboard ? FR_PLAN_CHECKERBOARD : 0;
+    pd.flags = (r->checkerboard ? FR_PLAN_CHECKERBOARD : 0) |
+               ((d->flags & FR_RECON_DETERMINISTIC) ? FR_PLAN_DETERMINISTIC : 0);
     st = fr_plan_create(&pd, &r->plan);
     // the pruned transform with fused crop + SoS where it is specialised for
     // G (faster than cuFFT + SoS there), or when asked for

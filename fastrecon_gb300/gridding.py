@@ -51,7 +51,8 @@ def grid_size(recon_size: int, overgrid_factor: float) -> int:
     return int(np.float32(recon_size) * np.float32(overgrid_factor))
 
 
-def _plan_desc(dim, grid_size, kernel_width, lut, tile, coil_group, chunk, checkerboard, tap_lists):
+def _plan_desc(dim, grid_size, kernel_width, lut, tile, coil_group, chunk, checkerboard, tap_lists,
+               deterministic=False):
     """fr_plan_desc over ``lut`` (a float32 array the caller keeps alive)."""
     d = capi.PlanDesc()
     d.dim = dim
@@ -63,7 +64,8 @@ def _plan_desc(dim, grid_size, kernel_width, lut, tile, coil_group, chunk, check
         d.tile[i] = int(tile[i]) if i < len(tile) else 0
     d.coil_group = coil_group
     d.chunk = chunk
-    d.flags = (capi.FR_PLAN_CHECKERBOARD if checkerboard else 0) | (0 if tap_lists else capi.FR_PLAN_NO_TAP_LISTS)
+    d.flags = ((capi.FR_PLAN_CHECKERBOARD if checkerboard else 0) | (0 if tap_lists else capi.FR_PLAN_NO_TAP_LISTS) |
+               (capi.FR_PLAN_DETERMINISTIC if deterministic else 0))
     return d
 
 
@@ -75,12 +77,13 @@ class GridPlan:
 
     def __init__(self, dim: int, grid_size: int, kernel_width: float = 4.0, lut=None, lut_length: int = 512,
                  overgrid_factor: float = 2.0, tile=(0, 0, 0), coil_group: int = 0, chunk: int = 0,
-                 checkerboard: bool = False, tap_lists: bool = True):
+                 checkerboard: bool = False, tap_lists: bool = True, deterministic: bool = False):
         self.lib = capi.load()
         if lut is None:
             lut = kb_lut(kernel_width, overgrid_factor, lut_length)
         self.lut = np.ascontiguousarray(lut, np.float32)
-        d = _plan_desc(dim, grid_size, kernel_width, self.lut, tile, coil_group, chunk, checkerboard, tap_lists)
+        d = _plan_desc(dim, grid_size, kernel_width, self.lut, tile, coil_group, chunk, checkerboard, tap_lists,
+                       deterministic)
         h = C.c_void_p()
         check(self.lib.fr_plan_create(C.byref(d), C.byref(h)), "fr_plan_create")
         self.h = h
@@ -356,7 +359,7 @@ class Recon:
     def __init__(self, dim: int, recon_size: int, overgrid_factor: float, channels: int, out_size=None,
                  kernel_width: float = 4.0, lut_length: int = 512, max_samples: int = 0, tile=(0, 0, 0),
                  coil_group: int = 0, deapodize: bool = False, use_cufft: bool = False, pruned_fft: bool = False,
-                 grid_budget: int = 0):
+                 grid_budget: int = 0, deterministic: bool = False):
         self.lib = capi.load()
         d = capi.ReconDesc()
         d.dim = dim
@@ -373,7 +376,8 @@ class Recon:
         d.max_samples = max_samples
         d.coil_group = coil_group
         d.flags = ((capi.FR_RECON_DEAPODIZE if deapodize else 0) | (capi.FR_RECON_CUFFT if use_cufft else 0) |
-                   (capi.FR_RECON_PRUNED_FFT if pruned_fft else 0))
+                   (capi.FR_RECON_PRUNED_FFT if pruned_fft else 0) |
+                   (capi.FR_RECON_DETERMINISTIC if deterministic else 0))
         d.grid_budget = grid_budget  # bytes of grid workspace: coils in slabs (0: all at once)
         h = C.c_void_p()
         check(self.lib.fr_recon_create(C.byref(d), C.byref(h)), "fr_recon_create")

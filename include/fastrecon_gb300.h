@@ -91,11 +91,19 @@ enum {
                                        scatter evaluates each bin record's
                                        kernel taps itself (saves ~170 bytes
                                        per 3D sample of device memory, slower) */
-    FR_PLAN_ACCUMULATE = 1u << 3    /* fr_grid adds the plan's samples to
+    FR_PLAN_ACCUMULATE = 1u << 3,   /* fr_grid adds the plan's samples to
                                        d_grid instead of overwriting it (cells
                                        of tiles without samples are left as
                                        they are): one grid from several plans
                                        over sample ranges of one trajectory */
+    FR_PLAN_DETERMINISTIC = 1u << 4 /* bit-reproducible grids: the records of
+                                       tiles split into several work items are
+                                       put in sample order after the bin fill
+                                       (the fill places them with atomics), so
+                                       each item holds the same records on
+                                       every run.  Applies to the tap-list
+                                       scatter; costs two short kernels and
+                                       16 bytes per bin record of scratch */
 };
 
 /* ReconData::normalizeTraj (ReconData.cpp:211-225) on the device: component
@@ -404,10 +412,11 @@ typedef struct fr_recon_s *fr_recon;
 enum {
     FR_RECON_DEAPODIZE = 1u << 0, /* divide by the kernel's image-domain apodization */
     FR_RECON_CUFFT = 1u << 1,     /* always the full cuFFT transform + crop/SoS kernel */
-    FR_RECON_PRUNED_FFT = 1u << 2 /* the pruned transform with fused crop + SoS (fr_fft_crop_sos)
+    FR_RECON_PRUNED_FFT = 1u << 2, /* the pruned transform with fused crop + SoS (fr_fft_crop_sos)
                                      wherever it applies (even G = 2^a 3^b 5^c <= 1024); by default
                                      it is used for the grid sizes it has specialised passes for
                                      (64, 128, 160, 192, 240, 256, 320, 384, 480, 512, 640, 768, 1024) */
+    FR_RECON_DETERMINISTIC = 1u << 3 /* plan with FR_PLAN_DETERMINISTIC: bit-reproducible images */
 };
 
 typedef struct {

@@ -145,3 +145,66 @@ def test_out_of_memory_paths_with_injected_failures(torch):
         os.environ.pop("FR_FAIL_ALLOC_BYTES", None)
     p, g = _grid(torch, c, c["kdata"])
     assert p.tap_words() > 0 and rel_l2(g, c["grid"]) <= TOL
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def test_deterministic_plans_repeat_bit_for_bit(torch, oracle):
+    """FR_PLAN_DETERMINISTIC: the records of split tiles are put in sample
+    order after the bin fill, so every work item holds the same records and
+    the grid repeats bit for bit across plans and runs -- here with small
+    work items (many split tiles, up to ~50 items per tile) and the
+    50,000-sample dense point; the grid still equals the reference at 1e-5."""
+    import fastrecon_gb300 as fr
+    c = load_case("koosh3d_small")
+    kd = torch.from_numpy(c["kdata"]).cuda()
+    dcf = torch.from_numpy(c["dcf"]).cuda()
+    traj = torch.from_numpy(c["traj"]).cuda()
+    grids = []
+    for _ in range(3):
+        p = fr.GridPlan(c["dim"], c["G"], c["W"], lut=c["lut"], chunk=512, deterministic=True)
+        p.set_trajectory(traj)
+        assert p.stats()["slots"] > 0 and p.tap_words() > 0
+        grids.append(p.grid(kd, dcf).cpu().numpy())
+        grids.append(p.grid(kd, dcf).cpu().numpy())
+    for g in grids[1:]:
+        assert np.array_equal(_bits(g), _bits(grids[0]))
+    assert rel_l2(grids[0], c["grid"]) <= TOL
+
+    rng = np.random.default_rng(9)
+    n = 50000
+    tr = np.zeros((n + 2, 4), np.float32)
+    tr[0, :3] = -0.5
+    tr[1, :3] = 0.49
+    tr[2:, :3] = 0.013
+    d2 = rng.uniform(0.5, 1.5, n + 2).astype(np.float32)
+    k2 = (rng.standard_normal((4, n + 2)) + 1j * rng.standard_normal((4, n + 2))).astype(np.complex64)
+    lut = fr.kb_lut(4.0, 1.5, 512)
+    outs = []
+    for _ in range(3):
+        p = fr.GridPlan(3, 24, 4.0, lut=lut, chunk=512, deterministic=True)
+        p.set_trajectory(torch.from_numpy(tr).cuda())
+        outs.append(p.grid(torch.from_numpy(k2).cuda(), torch.from_numpy(d2).cuda()).cpu().numpy())
+    for g in outs[1:]:
+        assert np.array_equal(_bits(g), _bits(outs[0]))
+    tn, _, _, _, _ = oracle.normalize_traj(tr, 3, 24)
+    want = oracle.grid_f64(tn, d2, k2, 3, 24, 4.0, lut)
+    ref = oracle.grid(tn, d2, k2, 3, 24, 4.0, lut, threads=4)
+    assert rel_l2(outs[0], want) <= max(1e-5, 2 * rel_l2(ref, want))
+
+
+def test_deterministic_recon_repeats_bit_for_bit(torch):
+    """The recon object with FR_RECON_DETERMINISTIC: the same image bits on
+    every run (default records per work item, split centre tiles)."""
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import synth
+    t = synth.kooshball_3d(4000, 128)
+    dcf = synth.ramp_dcf(t, 3, 2.0)
+    kd = synth.kspace(t, 3, 64, 8, seed=2, xp=torch, device="cuda")
+    td, dd = torch.from_numpy(t).cuda(), torch.from_numpy(dcf).cuda()
+    rec = fr.Recon(3, 64, 1.5, 8, max_samples=t.shape[0], deterministic=True)
+    imgs = [rec.run(td, dd, kd).cpu().numpy() for _ in range(4)]
+    for im in imgs[1:]:
+        assert np.array_equal(_bits(im), _bits(imgs[0]))
