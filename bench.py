@@ -141,6 +141,17 @@ def make_inputs(w, torch, device):
     return (torch.from_numpy(traj).to(device), torch.from_numpy(dcf).to(device), kd, np.float32)
 
 
+def scatter_kernel(taps: bool, coils: int) -> str:
+    """The scatter kernel the recon launches: with tap lists, the tap-lane
+    scatter for coil groups of 16 (9 coils and more) unless
+    FR_SCATTER_WARP_LISTS=1, the per-warp tap-list scatter otherwise."""
+    if not taps:
+        return "grid_tiles_kernel"
+    if coils > 8 and os.environ.get("FR_SCATTER_WARP_LISTS", "0") in ("", "0"):
+        return "grid_lanes_kernel"
+    return "grid_taps_kernel"
+
+
 def algorithmic_bytes(w):
     """Gridding algorithmic bytes per launch: coordinates (4d B) + DCF (4 B)
     per sample, 8 B per sample and coil, 8 B per grid cell and coil written
@@ -455,7 +466,7 @@ def run_ours(args, w):
     per_launch_ms = scatter_ms / max(scatter_n, 1)
     achieved = algo / (per_launch_ms / 1e3) / 1e9
     traffic = None
-    kernel = "grid_taps_kernel" if taps else "grid_tiles_kernel"
+    kernel = scatter_kernel(taps, C)
     tr_path = os.path.join(ROOT, "profiles", kernel.replace("_kernel", "") + "_traffic.txt")
     if os.path.exists(tr_path):
         for line in open(tr_path):

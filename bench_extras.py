@@ -116,7 +116,8 @@ def radial2d(torch, steps=50, warmup=5):
     scatter_ms, launches = rec.profile_read()
     rec.profile(False)
     G = 512
-    kern = "grid_taps_kernel" if rec.tap_words() > 0 else "grid_tiles_kernel"
+    from bench import scatter_kernel
+    kern = scatter_kernel(rec.tap_words() > 0, c)
     return {"value": n * c / (ms / 1e3) / 1e6, "unit": "Msamples/s", "ms_per_step": ms, "samples": n, "coils": c,
             "roofline": _roofline(n * (4 * 2 + 4) + n * c * 8 + c * G * G * 8, scatter_ms / max(launches, 1),
                                   kern + " (one launch per step, CUDA events)"),

@@ -294,6 +294,8 @@ int fr_plan_create(const fr_plan_desc *d, fr_plan *out)
         const char *cm = std::getenv("FR_KSPACE_COIL_MAJOR");
         p->kspace_sample_major = !(cm && std::atoi(cm) != 0);
         p->taps_enabled = !(d->flags & FR_PLAN_NO_TAP_LISTS);
+        const char *wl = std::getenv("FR_SCATTER_WARP_LISTS");
+        p->scatter_warp_lists = wl && std::atoi(wl) != 0;
     }
     {
         // exact when hw^2 is representable and sqrt rounds back to hw

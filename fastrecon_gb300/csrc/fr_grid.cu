@@ -865,6 +865,263 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tap-lane scatter (rows of 32 coil floats, the tap lists of the plan): each
+// lane owns two taps of one bin record and adds them for all 32 coil floats
+// of its coil group, so the tap's cell row and weight stay in the lane's
+// registers and no per-record tap list goes through shared memory.
+//
+// A warp takes 32 of its records at a time (a batch): their tap pairs are
+// numbered by a warp scan and dealt to the lanes 32 per pass, so a pass packs
+// the pairs of several records (a record's pairs are consecutive).  Each
+// record's 32 coil values (dcf * k, times the item's fixed-point scale) are
+// first staged in a 128-byte slot of the warp's staging area.
+//
+// Bank-conflict-free adds: at step t lane j adds coil float t ^ j of each of
+// its taps.  The tile is [cell][32] int32 with 128-byte rows, so the 32
+// lanes of one red.shared hit the 32 banks once each, whatever their cells;
+// the lane reads the same float t ^ j of its record's slot (again one bank
+// per lane).  The adds are those of grid_taps_kernel (same fixed-point
+// values), so a tile held by one work item grids to the same bits.
+// ---------------------------------------------------------------------------
+constexpr int kLaneWarps = 8;   // 256 threads per CTA
+constexpr int kLaneBatch = 32;  // records per warp batch (one per lane)
+
+// Shared-memory layout of grid_lanes_kernel from its 128-byte aligned base:
+// tile [K][32] int32 | weights [L] | per warp: value slots [32][32] floats,
+// record table [32] int4 {sample, first word | taps << 8, first pair, 0}.
+struct LaneSmem {
+    unsigned lutw, stage, table, end;
+};
+__host__ __device__ __forceinline__ LaneSmem lane_smem_layout(long long K, int L)
+{
+    LaneSmem m;
+    m.lutw = (unsigned)(K * 32 * 4);
+    m.stage = m.lutw + (unsigned)((L * 4 + 127) & ~127);
+    m.table = m.stage + (unsigned)(kLaneWarps * kLaneBatch * 128);
+    m.end = m.table + (unsigned)(kLaneWarps * kLaneBatch * 16);
+    return m;
+}
+
+__device__ __forceinline__ float lds_f32_v(unsigned a)
+{
+    float r;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(a));
+    return r;
+}
+
+// Flush of a [cell][32] tile (rows not swizzled): lane = (coil cl = lane & 15,
+// pair px = lane >> 4), so that one 8-byte shared load per lane covers the 32
+// banks and lanes cl, cl + 16 write the two halves of one 32-byte sector of
+// coil plane cl.  Units (tile row, two x pairs) are dealt to the warps.
+__device__ __forceinline__ void lanes_flush(const GridParams &P, unsigned acc, int cg, int ox, int oy, int oz, float inv)
+{
+    const int Tx = P.tile[0], Ty = P.tile[1], Tz = P.tile[2];
+    const int CG = P.coil_group;
+    const int ncl = min(CG, P.channels - cg * CG);
+    const size_t G = (size_t)P.G;
+    const int Gz = P.dim == 3 ? P.G : 1;
+    const size_t cells = P.dim == 3 ? G * G * G : G * G;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    float *gridf = P.grid;
+    if ((Tx % 4) == 0 && (P.G % 2) == 0 && ((reinterpret_cast<uintptr_t>(gridf) & 15) == 0)) {
+        const int cl = lane & 15, px = lane >> 4;
+        const int ppr = Tx / 4;  // x pair-pairs per row
+        const int units = Ty * Tz * ppr;
+        const size_t cstride4 = cells >> 1;
+        float4 *grid4 = reinterpret_cast<float4 *>(gridf) + (size_t)(cg * CG + cl) * cstride4;
+        for (int u = warp; u < units; u += nwarps) {
+            const int r = u / ppr, pp = u - r * ppr;
+            const int lx = 4 * pp + 2 * px;
+            const int gx = ox + lx, gy = oy + r % Ty, gz = oz + r / Ty;
+            if (cl >= ncl || gx >= P.G || gy >= P.G || gz >= Gz) continue;
+            const int i = r * Tx + lx;
+            const int2 a = lds_i32x2(acc + ((unsigned)i << 7) + ((unsigned)cl << 3));
+            const int2 b = lds_i32x2(acc + ((unsigned)(i + 1) << 7) + ((unsigned)cl << 3));
+            const float sa = P.checkerboard && ((gx + gy + gz) & 1) ? -inv : inv;
+            const float sb = P.checkerboard ? -sa : inv;
+            const float4 v = make_float4((float)a.x * sa, (float)a.y * sa, (float)b.x * sb, (float)b.y * sb);
+            put_cells(&grid4[(((size_t)gz * G + (size_t)gy) * G + (size_t)gx) >> 1], v, P.accumulate);
+        }
+        return;
+    }
+    const int K = P.K;
+    float2 *grid = reinterpret_cast<float2 *>(gridf);
+    for (int idx = threadIdx.x; idx < ncl * K; idx += blockDim.x) {
+        const int i = idx / ncl, cl = idx - i * ncl;
+        const int lx = i % Tx, r = i / Tx;
+        const int gx = ox + lx, gy = oy + r % Ty, gz = oz + r / Ty;
+        if (gx >= P.G || gy >= P.G || gz >= Gz) continue;
+        const int2 a = lds_i32x2(acc + ((unsigned)i << 7) + ((unsigned)cl << 3));
+        const float sg = P.checkerboard && ((gx + gy + gz) & 1) ? -inv : inv;
+        put_cells(&grid[(size_t)(cg * CG + cl) * cells + ((size_t)gz * G + (size_t)gy) * G + (size_t)gx],
+                  make_float2((float)a.x * sg, (float)a.y * sg), P.accumulate);
+    }
+}
+
+template <typename IT>
+__global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridParams P)
+{
+    extern __shared__ float4 smem_raw[];
+    float4 *smem4 = aligned_smem(smem_raw);
+    const WorkItem it = P.items[blockIdx.x];
+    const int cg = blockIdx.y;
+    const int K = P.K;
+    const int CG = P.coil_group;
+    const LaneSmem L_ = lane_smem_layout(K, P.L);
+    const unsigned acc = smem_addr(smem4);
+
+    const int t = it.tile;
+    const int ox = (t % P.ntile[0]) * P.tile[0];
+    const int oy = ((t / P.ntile[0]) % P.ntile[1]) * P.tile[1];
+    const int oz = (t / (P.ntile[0] * P.ntile[1])) * P.tile[2];
+    if (it.count == 0) {
+        if (!P.skip_empty) write_cell_group<32>(P, P.grid, acc, cg, ox, oy, oz, true, nullptr);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    float *lutw_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + L_.lutw);
+    for (int i = threadIdx.x; i < K * 8; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutw_s[i] = P.lutw[i];
+    const float inv = P.item_inv[blockIdx.x];
+    const float sc = __fdiv_rn(1.f, inv);  // exact: a power of two
+    __syncthreads();
+
+    const unsigned stage = acc + L_.stage + (unsigned)(warp * kLaneBatch * 128);
+    float4 *stage4 = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.stage) +
+                     warp * kLaneBatch * 8;
+    int4 *table4 = reinterpret_cast<int4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.table) + warp * kLaneBatch;
+    const int ncl = min(CG, P.channels - cg * CG);
+    const float *kt = P.kdata + 2 * (size_t)cg * CG;
+    const unsigned *taps = P.taps;
+    const IT tw = (IT)P.tap_words;
+    const IT vstride = (IT)(2 * P.kstride);
+    const unsigned cmask = (1u << kTapCellBits) - 1u;
+    const unsigned lane4 = (unsigned)lane << 2;
+
+    const int nrec = warp < it.count ? (it.count - warp + kLaneWarps - 1) / kLaneWarps : 0;
+    const unsigned long long *trecs = P.trecs + it.begin + warp;
+    // global loads run one step ahead of their use: the record words one
+    // batch ahead, the tap words of the next pass during the current pass's
+    // adds, and a batch's values all issued before the first is stored
+    auto load_rw = [&](int b0) -> unsigned long long {
+        const int k = b0 + lane;
+        return k < nrec ? __ldg(trecs + (size_t)kLaneWarps * k) : 0ull;
+    };
+    unsigned long long rw_next = load_rw(0);
+    for (int b0 = 0; b0 < nrec; b0 += kLaneBatch) {
+        // this lane's record of the batch: its tap pairs, their first number
+        const unsigned long long rw = rw_next;
+        rw_next = load_rw(b0 + kLaneBatch);
+        const int nt = (int)((rw >> 40) & 0xFF);
+        const int np = (nt + 1) >> 1;
+        const unsigned nz = __ballot_sync(0xffffffffu, np > 0);
+        int incl = np;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int excl = incl - np;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int nnz = __popc(nz);
+        if (np > 0) {
+            const int c = __popc(nz & ((1u << lane) - 1u));
+            table4[c] = make_int4((int)(unsigned)rw, (int)(((rw >> 32) & 0xFF) | ((unsigned)nt << 8)), excl, 0);
+        }
+        __syncwarp();
+        // stage the records' coil values: 8 lanes per record, one quad
+        // (2 coils) each, scaled by the item's fixed-point scale; quads past
+        // the group's last coil are zero
+        {
+            const int q = lane & 7;
+            const bool qok = 2 * q < ncl;
+            float4 vq[kLaneBatch / 4];
+#pragma unroll
+            for (int j = 0; j < kLaneBatch / 4; ++j) {
+                const int r = (lane >> 3) + 4 * j;
+                vq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r < nnz && qok) {
+                    const unsigned smp = (unsigned)table4[r].x;
+                    vq[j] = __ldg(reinterpret_cast<const float4 *>(kt + (IT)smp * vstride) + q);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kLaneBatch / 4; ++j) {
+                const int r = (lane >> 3) + 4 * j;
+                if (r < nnz)
+                    stage4[r * 8 + q] = make_float4(__fmul_rn(vq[j].x, sc), __fmul_rn(vq[j].y, sc),
+                                                    __fmul_rn(vq[j].z, sc), __fmul_rn(vq[j].w, sc));
+            }
+        }
+        __syncwarp();
+        // pass setup: the lane's pair number p0 + lane, its record (compact
+        // index cr), pair offset and tap words
+        int recbase = 0;
+        auto pass_setup = [&](int p0, int &cr, int &pi, int &ntr, unsigned &t0, unsigned &t1) {
+            // bit i of starts: a record's first pair is pair p0 + i
+            const bool in_pass = np > 0 && excl >= p0 && excl < p0 + 32;
+            const unsigned starts = __reduce_or_sync(0xffffffffu, in_pass ? 1u << (excl - p0) : 0u);
+            cr = recbase + __popc(starts & (0xffffffffu >> (31 - lane))) - 1;
+            recbase += __popc(starts);
+            pi = 0;
+            ntr = 0;
+            t0 = t1 = 0u;
+            if (p0 + lane < total) {
+                const int4 e = table4[cr];
+                ntr = e.y >> 8;
+                pi = 2 * (p0 + lane - e.z);
+                const IT tb = (IT)(unsigned)e.x * tw + (IT)(e.y & 0xFF) + (IT)pi;
+                t0 = __ldg(taps + tb);
+                if (pi + 1 < ntr) t1 = __ldg(taps + tb + 1);
+            }
+        };
+        int cr_n, pi_n, ntr_n;
+        unsigned t0_n, t1_n;
+        pass_setup(0, cr_n, pi_n, ntr_n, t0_n, t1_n);
+        for (int p0 = 0; p0 < total; p0 += 32) {
+            const int cr = cr_n, pi = pi_n, ntr = ntr_n;
+            const unsigned t0 = t0_n, t1 = t1_n;
+            if (p0 + 32 < total) pass_setup(p0 + 32, cr_n, pi_n, ntr_n, t0_n, t1_n);
+            if (p0 + lane < total) {
+                const bool has1 = pi + 1 < ntr;
+                const unsigned c0 = min(t0 & cmask, (unsigned)(K - 1)), c1 = min(t1 & cmask, (unsigned)(K - 1));
+                const float w0 = lutw_s[min(t0 >> kTapCellBits, (unsigned)(P.L - 1))];
+                const float w1 = has1 ? lutw_s[min(t1 >> kTapCellBits, (unsigned)(P.L - 1))] : 0.f;
+                const unsigned a0 = (acc + (c0 << 7)) | lane4, a1 = (acc + (c1 << 7)) | lane4;
+                const unsigned va = (stage + ((unsigned)cr << 7)) | lane4;
+                float v[32];
+#pragma unroll
+                for (int f = 0; f < 32; ++f) v[f] = lds_f32_v(va ^ ((unsigned)f << 2));
+#pragma unroll
+                for (int f = 0; f < 32; ++f) red_add_fx(a0 ^ ((unsigned)f << 2), w0, v[f]);
+                if (has1) {
+#pragma unroll
+                    for (int f = 0; f < 32; ++f) red_add_fx(a1 ^ ((unsigned)f << 2), w1, v[f]);
+                }
+            }
+        }
+        __syncwarp();  // the next batch rewrites the table and the slots
+    }
+    __syncthreads();
+    if (it.slot < 0) {
+        lanes_flush(P, acc, cg, ox, oy, oz, inv);
+    } else {
+        // partial tile in the [cell][32] layout the reduction reads (float g
+        // of cell c at g ^ ((c & 15) << 1)): float4 q of a row is plain quad
+        // q ^ ((c & 15) >> 1), pairs swapped for odd cells
+        float4 *dst = reinterpret_cast<float4 *>(P.partials + ((size_t)it.slot * P.ngroups + cg) * (size_t)K * 32);
+        for (int i4 = threadIdx.x; i4 < K * 8; i4 += blockDim.x) {
+            const int c = i4 >> 3, q = i4 & 7;
+            int4 a = lds_s32x4(acc + ((unsigned)c << 7) + ((unsigned)(q ^ ((c & 15) >> 1)) << 4));
+            if (c & 1) a = make_int4(a.z, a.w, a.x, a.y);
+            dst[i4] = make_float4((float)a.x * inv, (float)a.y * inv, (float)a.z * inv, (float)a.w * inv);
+        }
+    }
+}
+
 // Per work item, from the per-sample bounds (mag[s] >= every |dcf * k| of
 // sample s), one warp per item: the sum and the maximum over the item's
 // records with taps.  The sum is exact and independent of the records'
@@ -1117,13 +1374,19 @@ int launch_taps(fr_plan p, const GridParams &P, long long nitems, long long nspl
             bound, nitems, P.lut_absmax, const_cast<float *>(P.item_inv));
         FR_CHECK_LAUNCH("item_inv_kernel");
     }
-    const TapSmem m = tap_smem_layout(P.K, R, P.L);
-    const size_t smem = m.end + 128;
-    if (smem > 227 * 1024) return fail(FR_ERR_UNSUPPORTED, "tap-list scatter does not fit in shared memory");
     // 32-bit indices when the tap words and sample-major values allow them
     const bool idx32 = (double)P.n * (double)P.tap_words < 2147483647.0 &&
                        (double)P.n * (double)(2 * P.kstride) < 2147483647.0;
-    auto kern = idx32 ? grid_taps_kernel<R, unsigned> : grid_taps_kernel<R, unsigned long long>;
+    // rows of 32 coil floats: the tap-lane scatter, unless a plan asks for
+    // the per-warp tap lists
+    const LaneSmem lm = lane_smem_layout(P.K, P.L);
+    const bool lanes = R == 32 && !p->scatter_warp_lists && lm.end + 128 <= 227 * 1024 && (P.kstride % 2) == 0;
+    const TapSmem m = tap_smem_layout(P.K, R, P.L);
+    const size_t smem = lanes ? lm.end + 128 : m.end + 128;
+    if (smem > 227 * 1024) return fail(FR_ERR_UNSUPPORTED, "tap-list scatter does not fit in shared memory");
+    auto kern = lanes ? (idx32 ? grid_lanes_kernel<unsigned> : grid_lanes_kernel<unsigned long long>)
+                      : (idx32 ? grid_taps_kernel<R, unsigned> : grid_taps_kernel<R, unsigned long long>);
+    const int threads = lanes ? kLaneWarps * 32 : kWarps * 32;
     if (smem > 48 * 1024) FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)nitems, (unsigned)P.ngroups);
     cudaEvent_t *ev = nullptr;
@@ -1139,8 +1402,8 @@ int launch_taps(fr_plan p, const GridParams &P, long long nitems, long long nspl
         p->prof_used++;
         FR_CUDA(cudaEventRecord(ev[0], s));
     }
-    kern<<<grid, kWarps * 32, smem, s>>>(P);
-    FR_CHECK_LAUNCH("grid_taps_kernel");
+    kern<<<grid, threads, smem, s>>>(P);
+    FR_CHECK_LAUNCH(lanes ? "grid_lanes_kernel" : "grid_taps_kernel");
     if (ev) FR_CUDA(cudaEventRecord(ev[1], s));
     return launch_reduce<R>(P, nsplits, s);
 }

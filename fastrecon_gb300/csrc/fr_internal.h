@@ -132,6 +132,7 @@ struct fr_plan_s {
     // per tile it touches, in the plan's tile-walk order).  Tap word:
     // tile-local cell | LUT index << 13.
     bool taps_enabled = true;  // cleared by FR_PLAN_NO_TAP_LISTS
+    bool scatter_warp_lists = false;  // FR_SCATTER_WARP_LISTS=1: per-warp tap lists instead of tap lanes
     int tap_words = 0;         // 0: this plan has no tap lists
     int tap_layout_words = 0;  // tap_slot_layout of this plan (computed once)
     fr::DevBuf taps;           // n x tap_words words
