@@ -381,6 +381,14 @@ __device__ __forceinline__ int tap_lut_index(float s2, const float4 *__restrict_
     const int k0 = (int)fminf(fmaf(a, kc, 0.25f), (float)(L - 1));
     return k0 + (s2 >= __ldg(&lut_e[k0].x) ? 1 : 0);
 }
+// The same with the thresholds thr[k] = lut_e[k].x staged in shared memory.
+__device__ __forceinline__ int tap_lut_index_s(float s2, const float *thr, float kc, int L)
+{
+    float a;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(s2));
+    const int k0 = (int)fminf(fmaf(a, kc, 0.25f), (float)(L - 1));
+    return k0 + (s2 >= thr[k0] ? 1 : 0);
+}
 
 // Pass 3 with tap lists: the records of fill_kernel, and for each record the
 // taps of the sample inside the record's tile, evaluated with the
@@ -442,6 +450,59 @@ __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg,
                             slot[wi] = (unsigned)(rowzy + lx[i]) |
                                        ((unsigned)tap_lut_index(s2, tg.lut_e, tg.kc, tg.L) << kTapCellBits);
                     }
+                }
+            }
+        }
+    }
+}
+
+// The same walk for samples whose range touches at most 8 tiles, with the
+// per-record tap counts and first words packed as bytes in two 64-bit
+// registers (byte j: record j) instead of shared-memory counters: no
+// load-add-store chain through shared memory per candidate cell, and the LUT
+// thresholds read from shared memory.  The words and their order are those
+// of sample_taps.
+template <int XR>
+__device__ __forceinline__ void sample_taps_pk(const BinGeom &g, const TapGeom &tg, const float *thr, const float *c,
+                                               const int *s, const int *e, const TileWalk &w, bool place,
+                                               unsigned long long &cnt, unsigned long long off, unsigned *slot)
+{
+    float dx2[XR];
+    int jx[XR], lx[XR];
+#pragma unroll
+    for (int i = 0; i < XR; ++i) {
+        const int x = s[0] + i;
+        const float dx = __fsub_rn((float)x, c[0]);
+        dx2[i] = x <= e[0] ? __fmul_rn(dx, dx) : __int_as_float(0x7f800000);
+        jx[i] = tile_div(g, x, 0) - w.lo[0];
+        lx[i] = x - (w.lo[0] + jx[i]) * g.tile[0];
+    }
+    float fz = (float)s[2];
+    for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
+        const float dz = g.dim == 3 ? __fsub_rn(fz, c[2]) : 0.f;
+        const float dz2 = __fmul_rn(dz, dz);
+        const int jz = tile_div(g, z, 2) - w.lo[2];
+        const int lz = z - (w.lo[2] + jz) * g.tile[2];
+        float fy = (float)s[1];
+        for (int y = s[1]; y <= e[1]; ++y, fy = __fadd_rn(fy, 1.f)) {
+            const float dy = __fsub_rn(fy, c[1]);
+            const float dzy = __fadd_rn(dz2, __fmul_rn(dy, dy));
+            const int jy = tile_div(g, y, 1) - w.lo[1];
+            const int ly = y - (w.lo[1] + jy) * g.tile[1];
+            const int jzy = (jz * w.n[1] + jy) * w.n[0];
+            const int rowzy = (lz * g.tile[1] + ly) * g.tile[0];
+#pragma unroll
+            for (int i = 0; i < XR; ++i) {
+                const float s2 = __fadd_rn(dzy, dx2[i]);
+                if (s2 < tg.smax) {
+                    const unsigned sh = 8u * (unsigned)(jzy + jx[i]);
+                    if (place) {
+                        const int wi = (int)(((off >> sh) & 255ull) + ((cnt >> sh) & 255ull));
+                        if (wi < tg.words)
+                            slot[wi] = (unsigned)(rowzy + lx[i]) |
+                                       ((unsigned)tap_lut_index_s(s2, thr, tg.kc, tg.L) << kTapCellBits);
+                    }
+                    cnt += 1ull << sh;
                 }
             }
         }
@@ -535,6 +596,121 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_kernel(const float4 *_
             // word wi = 4 qd + k of the block's slots is word (wi mod W) of
             // sample wi / W: kept as a (sample, word) pair advanced without
             // divisions (one division to start, then steps of 4 kFillThreads)
+            const int step = 4 * kFillThreads, sq = step / W, sr = step - sq * W;
+            int smp = (4 * threadIdx.x) / W, wd = 4 * threadIdx.x - smp * W;
+            for (int qd = threadIdx.x; qd < total / 4; qd += kFillThreads) {
+                unsigned v[4];
+                int sm = smp, wk = wd;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    v[k] = stage[sm * S + wk];
+                    if (++wk == W) {
+                        wk = 0;
+                        ++sm;
+                    }
+                }
+                dst[qd] = make_uint4(v[0], v[1], v[2], v[3]);
+                smp += sq;
+                wd += sr;
+                if (wd >= W) {
+                    wd -= W;
+                    ++smp;
+                }
+            }
+        }
+        for (int wi = (total & ~3) + threadIdx.x; wi < total; wi += kFillThreads) {
+            const int smp = wi / W;
+            tg.taps[base * (size_t)W + wi] = stage[smp * S + (wi - smp * W)];
+        }
+        __syncthreads();
+    }
+}
+
+// fill_taps_kernel for samples touching at most 8 tiles (the 3D 4-wide
+// kernel on 8^3 tiles, 2D on 32^2): counts and first words in registers
+// (sample_taps_pk), LUT thresholds staged in shared memory after the slots.
+template <int XR>
+__global__ void __launch_bounds__(kFillThreads) fill_taps_pk_kernel(const float4 *__restrict__ traj, size_t n,
+                                                                    BinGeom g, TapGeom tg,
+                                                                    const long long *__restrict__ stripe_base,
+                                                                    int *__restrict__ tile_fill,
+                                                                    unsigned long long *__restrict__ recs)
+{
+    extern __shared__ unsigned stage[];
+    const int S = tg.words | 1;
+    const int lane = threadIdx.x & 31;
+    unsigned *mine = stage + threadIdx.x * S;
+    float *thr = reinterpret_cast<float *>(stage + kFillThreads * S);
+    for (int k = threadIdx.x; k < tg.L; k += kFillThreads) thr[k] = __ldg(&tg.lut_e[k].x);
+    __syncthreads();
+    for (size_t base = blockIdx.x * (size_t)kFillThreads; base < n; base += (size_t)gridDim.x * kFillThreads) {
+        size_t i = base + threadIdx.x;
+        TileWalk w;
+        int s[3] = {0, 0, 0}, e[3] = {0, 0, 0};
+        float c[3] = {0.f, 0.f, 0.f};
+        int cnt_t = 0;
+        if (i < n) {
+            float4 q = traj[i];
+            cnt_t = sample_tiles(g, q, w, s, e);
+            c[0] = q.x;
+            c[1] = q.y;
+            c[2] = q.z;
+        } else {
+            w.lo[0] = w.lo[1] = w.lo[2] = 0;
+            w.n[0] = w.n[1] = w.n[2] = 1;
+        }
+        // taps per record (byte j of cnt), each record's first word (byte j
+        // of off), then the taps
+        unsigned long long cnt = 0ull, off = 0ull;
+        const bool narrow = e[0] - s[0] + 1 < XR;
+        if (cnt_t > 0) {
+            if (narrow)
+                sample_taps_pk<XR - 1>(g, tg, thr, c, s, e, w, false, cnt, 0ull, mine);
+            else
+                sample_taps_pk<XR>(g, tg, thr, c, s, e, w, false, cnt, 0ull, mine);
+        }
+        int tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            off |= (unsigned long long)min(tot, 255) << (8 * j);
+            tot += (int)((cnt >> (8 * j)) & 255ull);
+        }
+        if (tot <= tg.words && cnt_t > 0) {
+            unsigned long long k = 0ull;  // taps placed per record
+            if (narrow)
+                sample_taps_pk<XR - 1>(g, tg, thr, c, s, e, w, true, k, off, mine);
+            else
+                sample_taps_pk<XR>(g, tg, thr, c, s, e, w, true, k, off, mine);
+        }
+        if (tot > tg.words) *tg.err = FR_ERR_CAPACITY;  // never: the slot bounds every sample's taps
+
+        const int stripe = stripe_of(base + threadIdx.x - lane);
+        int maxcnt = __reduce_max_sync(0xffffffffu, cnt_t);
+        for (int j = 0; j < maxcnt; ++j, w.next()) {
+            bool valid = j < cnt_t;
+            int t = valid ? w.tile(g) : -1 - lane;
+            int run, head_lane;
+            lane_runs(t, lane, run, head_lane);
+            int basepos = 0;
+            const int ts = t * kStripes + stripe;
+            if (valid && lane == head_lane) basepos = atomicAdd(&tile_fill[ts], run);
+            basepos = __shfl_sync(0xffffffffu, basepos, head_lane);
+            if (valid) {
+                long long pos = stripe_base[ts] + basepos + (lane - head_lane);
+                unsigned box = tile_box(g, c, s, e, w.lo[0] + w.jx, w.lo[1] + w.jy, w.lo[2] + w.jz);
+                recs[pos] = ((unsigned long long)box << 32) | (unsigned long long)i;
+                const unsigned sh = 8u * (unsigned)j;
+                const unsigned long long ntap = tot > tg.words ? 0ull : (cnt >> sh) & 255ull;  // a dropped run (never) has no taps
+                tg.trecs[pos] = (unsigned long long)i | (((off >> sh) & 255ull) << 32) | (ntap << 40);
+            }
+        }
+        __syncthreads();
+        // the block's slots are words [base * words, (base + nv) * words):
+        // 16-byte aligned (base is a multiple of kFillThreads), copied as uint4
+        const int nv = (int)min((size_t)kFillThreads, n - base);
+        const int W = tg.words, total = nv * W;
+        uint4 *dst = reinterpret_cast<uint4 *>(tg.taps + base * (size_t)W);
+        {
             const int step = 4 * kFillThreads, sq = step / W, sr = step - sq * W;
             int smp = (4 * threadIdx.x) / W, wd = 4 * threadIdx.x - smp * W;
             for (int qd = threadIdx.x; qd < total / 4; qd += kFillThreads) {
@@ -984,18 +1160,21 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         tg.recmax = recmax;
         // slot staging plus 2 bytes per possible record: 4 CTAs of 256 per SM
         // for the 3D 4-wide kernel (42 words, 8 records)
-        const size_t smem = (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * recmax);
-        // cells of a sample's range along x: at most floor(2 hw) + 1; the
-        // mask walk when a range touches at most 2 tiles per axis and its
-        // taps fit one 64-bit mask
+        // (packed-counter form when a sample touches at most 8 tiles: slot
+        // staging plus the L thresholds)
+        const bool pk = recmax <= 8;
+        const size_t smem = pk ? (size_t)kFillThreads * (size_t)(p->tap_words | 1) * 4 + (size_t)p->L * 4
+                               : (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * recmax);
+        // cells of a sample's range along x: at most floor(2 hw) + 1
         const int Fx = (int)std::floor(2.0 * p->hw) + 1;
-        auto kern = Fx <= 5 ? fill_taps_kernel<5> : fill_taps_kernel<9>;
+        auto kern = pk ? (Fx <= 5 ? fill_taps_pk_kernel<5> : fill_taps_pk_kernel<9>)
+                       : (Fx <= 5 ? fill_taps_kernel<5> : fill_taps_kernel<9>);
         if ((int)std::floor(2.0 * p->hw) + 1 > 9) return fail(FR_ERR_UNSUPPORTED, "tap lists: kernel too wide");
         if (smem > 48 * 1024)
             FR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<grid_blocks(n, kFillThreads), kFillThreads, smem, s>>>(
             traj, n, g, tg, p->stripe_base.as<long long>(), p->tile_fill.as<int>(), p->pairs.as<unsigned long long>());
-        FR_CHECK_LAUNCH("fill_taps_kernel");
+        FR_CHECK_LAUNCH(pk ? "fill_taps_pk_kernel" : "fill_taps_kernel");
     } else if (n > 0) {
         fill_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(traj, n, g, p->stripe_base.as<long long>(), p->tile_fill.as<int>(),
                                                         p->pairs.as<unsigned long long>());
