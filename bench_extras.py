@@ -162,7 +162,7 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
     # the grid is flushed with the fftShift checkerboard: pruned FFT + crop + SoS
     crop_sos = fr.gridding.CropSoS(3, G, coils, out_size)
     modes = ["pipe", "learned", "recon_only"] + [f"learned_refined_{k}" for k in refine]
-    imgs = {m: torch.empty((volumes, recon ** 3), dtype=torch.float32, device="cuda") for m in modes}
+    imgs = {m: torch.empty((volumes, recon ** 3), dtype=torch.float32, device="cuda") for m in modes + ["pipe_40"]}
     lib = fr.load()
 
     def run(mode, s):
@@ -177,10 +177,11 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
                                   "fr_dcf_pipe")
             elif mode == "recon_only":  # the recon with a DCF already at hand: the speed-up's ceiling
                 V["w"].fill_(1.0)
-            else:
+            else:  # "pipe": 20 Pipe-Menon iterations from uniform weights; "pipe_40": 40
                 V["w"].fill_(1.0)
-                fr.capi.check(lib.fr_dcf_pipe(V["plan"].h, 20, C.c_void_p(V["w"].data_ptr()),
-                                              C.c_void_p(s.cuda_stream)), "fr_dcf_pipe")
+                fr.capi.check(lib.fr_dcf_pipe(V["plan"].h, 40 if mode == "pipe_40" else 20,
+                                              C.c_void_p(V["w"].data_ptr()), C.c_void_p(s.cuda_stream)),
+                              "fr_dcf_pipe")
             V["plan"].grid(V["kd"], V["w"], out=grid, stream=s)
             crop_sos(grid, stream=s, out=imgs[mode][i])
 
@@ -196,6 +197,13 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
             ms = _ms(torch, g.replay, steps, warmup, s)
         res[mode] = ms
         del g
+    # the iterated DCF's own convergence: the 20-iteration recon against a
+    # 40-iteration one (untimed), and the network against both
+    with torch.cuda.stream(s):
+        run("pipe_40", s)
+        s.synchronize()
+    conv = [_nrmse(torch, imgs["pipe"][i], imgs["pipe_40"][i]) for i in range(volumes)]
+    nr40 = [_nrmse(torch, imgs["learned"][i], imgs["pipe_40"][i]) for i in range(volumes)]
     nr = [_nrmse(torch, imgs["learned"][i], imgs["pipe"][i]) for i in range(volumes)]
     refined = []
     for k in refine:
@@ -219,6 +227,12 @@ def learned_vs_pipe(torch, steps=3, warmup=1, volumes=8, coils=32, recon=256, os
                                "nrmse_median": at1["nrmse_median"]} if at1 else
                               {"variant": None, "reached": False,
                                "best_nrmse_median": min(c["nrmse_median"] for c in cands)}),
+            "pipe_convergence": {"nrmse_20_vs_40_median": float(np.median(conv)),
+                                 "nrmse_20_vs_40_max": float(np.max(conv)),
+                                 "learned_vs_40_median": float(np.median(nr40)),
+                                 "note": "image NRMSE of the 20-iteration Pipe-Menon recon against a 40-iteration "
+                                         "one (both from uniform weights), and of the network's recon against the "
+                                         "40-iteration one"},
             "recon_only_ms": res["recon_only"],
             "speedup_ceiling": res["pipe"] / res["recon_only"],
             "volumes": volumes,
