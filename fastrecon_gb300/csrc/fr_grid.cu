@@ -874,8 +874,10 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 // A warp takes 32 of its records at a time (a batch): their tap pairs are
 // numbered by a warp scan and dealt to the lanes 32 per pass, so a pass packs
 // the pairs of several records (a record's pairs are consecutive).  Each
-// record's 32 coil values (dcf * k, times the item's fixed-point scale) are
-// first staged in a 128-byte slot of the warp's staging area.
+// record's 32 coil values (dcf * k) are first copied into a 128-byte slot of
+// the warp's staging area by a bulk (TMA) copy, issued by the lane holding
+// the record and completing on the warp's mbarrier; the item's fixed-point
+// scale goes on the weights.
 //
 // Bank-conflict-free adds: at step t lane j adds coil float t ^ j of each of
 // its taps.  The tile is [cell][32] int32 with 128-byte rows, so the 32
@@ -889,9 +891,10 @@ constexpr int kLaneBatch = 32;  // records per warp batch (one per lane)
 
 // Shared-memory layout of grid_lanes_kernel from its 128-byte aligned base:
 // tile [K][32] int32 | weights [L] | per warp: value slots [32][32] floats,
-// record table [32] int4 {sample, first word | taps << 8, first pair, 0}.
+// record table [32] int4 {sample, first word | taps << 8, first pair, 0} |
+// per warp one mbarrier (8 bytes).
 struct LaneSmem {
-    unsigned lutw, stage, table, end;
+    unsigned lutw, stage, table, mbar, end;
 };
 __host__ __device__ __forceinline__ LaneSmem lane_smem_layout(long long K, int L)
 {
@@ -899,7 +902,8 @@ __host__ __device__ __forceinline__ LaneSmem lane_smem_layout(long long K, int L
     m.lutw = (unsigned)(K * 32 * 4);
     m.stage = m.lutw + (unsigned)((L * 4 + 127) & ~127);
     m.table = m.stage + (unsigned)(kLaneWarps * kLaneBatch * 128);
-    m.end = m.table + (unsigned)(kLaneWarps * kLaneBatch * 16);
+    m.mbar = m.table + (unsigned)(kLaneWarps * kLaneBatch * 16);
+    m.end = m.mbar + (unsigned)(kLaneWarps * 8);
     return m;
 }
 
@@ -908,6 +912,43 @@ __device__ __forceinline__ float lds_f32_v(unsigned a)
     float r;
     asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(a));
     return r;
+}
+
+// Bulk copies of the records' coil values into the warp's slots, completing
+// on the warp's mbarrier (the copies are issued by the lanes holding the
+// records, one 16..128-byte copy each; global source and shared slot 16-byte
+// aligned, sizes a multiple of 16).
+__device__ __forceinline__ void mbar_init(unsigned mbar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned mbar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(unsigned dst, const void *src, unsigned bytes, unsigned mbar)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the slot was last read by plain loads
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+// Waits (non-blocking polls, bounded: about 2^20 polls with short sleeps,
+// tens of milliseconds) for the phase of the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity)
+{
+    for (int i = 0; i < (1 << 20); ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (i >= 32) __nanosleep(32);
+    }
+    return false;
 }
 
 // Flush of a [cell][32] tile (rows not swizzled): lane = (coil cl = lane & 15,
@@ -983,17 +1024,26 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     float *lutw_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + L_.lutw);
+    // the tile and the value slots start at zero (a slot's coils past the
+    // group's last are never copied)
     for (int i = threadIdx.x; i < K * 8; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 *stage_all = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.stage);
+    for (int i = threadIdx.x; i < kLaneWarps * kLaneBatch * 8; i += blockDim.x)
+        stage_all[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutw_s[i] = P.lutw[i];
     const float inv = P.item_inv[blockIdx.x];
     const float sc = __fdiv_rn(1.f, inv);  // exact: a power of two
+    const unsigned mbar = acc + L_.mbar + 8u * (unsigned)warp;
+    if (lane == 0) mbar_init(mbar);
     __syncthreads();
 
     const unsigned stage = acc + L_.stage + (unsigned)(warp * kLaneBatch * 128);
-    float4 *stage4 = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.stage) +
-                     warp * kLaneBatch * 8;
     int4 *table4 = reinterpret_cast<int4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.table) + warp * kLaneBatch;
     const int ncl = min(CG, P.channels - cg * CG);
+    // bytes of a record's coil values: whole coil pairs (an odd count's pad
+    // coil is zero in the sample-major copy)
+    const unsigned vbytes = 16u * (unsigned)((ncl + 1) >> 1);
+    unsigned parity = 0u;
     const float *kt = P.kdata + 2 * (size_t)cg * CG;
     const unsigned *taps = P.taps;
     const IT tw = (IT)P.tap_words;
@@ -1027,33 +1077,16 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
         const int excl = incl - np;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         const int nnz = __popc(nz);
-        if (np > 0) {
-            const int c = __popc(nz & ((1u << lane) - 1u));
-            table4[c] = make_int4((int)(unsigned)rw, (int)(((rw >> 32) & 0xFF) | ((unsigned)nt << 8)), excl, 0);
-        }
-        __syncwarp();
-        // stage the records' coil values: 8 lanes per record, one quad
-        // (2 coils) each, scaled by the item's fixed-point scale; quads past
-        // the group's last coil are zero
-        {
-            const int q = lane & 7;
-            const bool qok = 2 * q < ncl;
-            float4 vq[kLaneBatch / 4];
-#pragma unroll
-            for (int j = 0; j < kLaneBatch / 4; ++j) {
-                const int r = (lane >> 3) + 4 * j;
-                vq[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (r < nnz && qok) {
-                    const unsigned smp = (unsigned)table4[r].x;
-                    vq[j] = __ldg(reinterpret_cast<const float4 *>(kt + (IT)smp * vstride) + q);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < kLaneBatch / 4; ++j) {
-                const int r = (lane >> 3) + 4 * j;
-                if (r < nnz)
-                    stage4[r * 8 + q] = make_float4(__fmul_rn(vq[j].x, sc), __fmul_rn(vq[j].y, sc),
-                                                    __fmul_rn(vq[j].z, sc), __fmul_rn(vq[j].w, sc));
+        // the records' coil values (dcf * k) into the slots by bulk copies,
+        // slot c for the c-th record with taps: lane 0 arms the mbarrier with
+        // the batch's bytes before any copy is issued
+        if (nnz > 0) {
+            if (lane == 0) mbar_expect_tx(mbar, (unsigned)nnz * vbytes);
+            __syncwarp();
+            if (np > 0) {
+                const int c = __popc(nz & ((1u << lane) - 1u));
+                table4[c] = make_int4((int)(unsigned)rw, (int)(((rw >> 32) & 0xFF) | ((unsigned)nt << 8)), excl, 0);
+                bulk_copy_g2s(stage + ((unsigned)c << 7), kt + (IT)(unsigned)rw * vstride, vbytes, mbar);
             }
         }
         __syncwarp();
@@ -1080,7 +1113,16 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
         };
         int cr_n, pi_n, ntr_n;
         unsigned t0_n, t1_n;
-        pass_setup(0, cr_n, pi_n, ntr_n, t0_n, t1_n);
+        pass_setup(0, cr_n, pi_n, ntr_n, t0_n, t1_n);  // the first pass's tap words load during the copies
+        if (nnz > 0) {
+            if (!mbar_wait(mbar, parity)) {
+                // a copy that never lands: report it and wait once more for
+                // the copies in flight before the slots are read
+                if (lane == 0 && P.err) atomicExch(P.err, FR_ERR_DEVICE_TIMEOUT);
+                mbar_wait(mbar, parity);
+            }
+            parity ^= 1u;
+        }
         for (int p0 = 0; p0 < total; p0 += 32) {
             const int cr = cr_n, pi = pi_n, ntr = ntr_n;
             const unsigned t0 = t0_n, t1 = t1_n;
@@ -1088,8 +1130,10 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
             if (p0 + lane < total) {
                 const bool has1 = pi + 1 < ntr;
                 const unsigned c0 = min(t0 & cmask, (unsigned)(K - 1)), c1 = min(t1 & cmask, (unsigned)(K - 1));
-                const float w0 = lutw_s[min(t0 >> kTapCellBits, (unsigned)(P.L - 1))];
-                const float w1 = has1 ? lutw_s[min(t1 >> kTapCellBits, (unsigned)(P.L - 1))] : 0.f;
+                // the item's power-of-two scale on the weights (exact: the
+                // same products w * v * S as scaling the values)
+                const float w0 = __fmul_rn(lutw_s[min(t0 >> kTapCellBits, (unsigned)(P.L - 1))], sc);
+                const float w1 = has1 ? __fmul_rn(lutw_s[min(t1 >> kTapCellBits, (unsigned)(P.L - 1))], sc) : 0.f;
                 const unsigned a0 = (acc + (c0 << 7)) | lane4, a1 = (acc + (c1 << 7)) | lane4;
                 const unsigned va = (stage + ((unsigned)cr << 7)) | lane4;
                 float v[32];
@@ -1510,8 +1554,10 @@ int grid_run(fr_plan p, const float *d_kdata, const float *d_dcf, int channels, 
     if (p->err_host && *p->err_host) {  // a kernel of an earlier call found an internal error
         const int e = *p->err_host;
         *p->err_host = 0;
-        return fail(e, "the plan's tap lists overflowed a sample slot (internal error)");
+        return fail(e, e == FR_ERR_DEVICE_TIMEOUT ? "a bulk copy of the scatter never completed (an earlier call)"
+                                                  : "the plan's tap lists overflowed a sample slot (internal error)");
     }
+    P.err = p->err_dev;
     // the tap-list scatter reads each record's coil values from the
     // sample-major copy; the geometry scatter uses the copy from 4 coils on
     const bool taps = p->tap_words > 0 && R <= 32;
