@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 // of its coil group, so the tap's cell row and weight stay in the lane's
 // registers and no per-record tap list goes through shared memory.
 //
-// A warp takes 32 of its records at a time (a batch): their tap pairs are
+// A warp holds 32 of its records at a time (a window): their tap pairs are
 // numbered by a warp scan and dealt to the lanes 32 per pass, so a pass packs
 // the pairs of several records (a record's pairs are consecutive).  Each
 // record's 32 coil values (dcf * k) are first copied into a 128-byte slot of
@@ -887,7 +887,7 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 // values), so a tile held by one work item grids to the same bits.
 // ---------------------------------------------------------------------------
 constexpr int kLaneWarps = 8;   // 256 threads per CTA
-constexpr int kLaneBatch = 32;  // records per warp batch (one per lane)
+constexpr int kLaneBatch = 32;  // records per warp window (one per lane)
 
 // Shared-memory layout of grid_lanes_kernel from its 128-byte aligned base:
 // tile [K][32] int32 | weights [L] | per warp: value slots [32][32] floats,
@@ -1053,18 +1053,22 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
 
     const int nrec = warp < it.count ? (it.count - warp + kLaneWarps - 1) / kLaneWarps : 0;
     const unsigned long long *trecs = P.trecs + it.begin + warp;
-    // global loads run one step ahead of their use: the record words one
-    // batch ahead, the tap words of the next pass during the current pass's
-    // adds, and a batch's values all issued before the first is stored
-    auto load_rw = [&](int b0) -> unsigned long long {
-        const int k = b0 + lane;
+    // global loads run one step ahead of their use: the record words after
+    // the window while it runs, the tap words of the next pass during the
+    // current pass's adds, the first pass's tap words while the window's
+    // bulk copies are in flight
+    auto load_rw = [&](int k0) -> unsigned long long {
+        const int k = k0 + lane;
         return k < nrec ? __ldg(trecs + (size_t)kLaneWarps * k) : 0ull;
     };
-    unsigned long long rw_next = load_rw(0);
-    for (int b0 = 0; b0 < nrec; b0 += kLaneBatch) {
-        // this lane's record of the batch: its tap pairs, their first number
-        const unsigned long long rw = rw_next;
-        rw_next = load_rw(b0 + kLaneBatch);
+    // Records go through a window of 32, one per lane.  A window processes
+    // only whole passes of 32 tap pairs (the warp's last window: all its
+    // pairs); the records it finished leave, the rest (the first possibly
+    // part-done: its first tap word and tap count advanced past the done
+    // pairs) move to the front and the window fills up from the next records.
+    unsigned long long rw = load_rw(0), rw_next = load_rw(kLaneBatch);
+    for (int wbase = 0; wbase < nrec;) {
+        // this lane's record of the window: its tap pairs, their first number
         const int nt = (int)((rw >> 40) & 0xFF);
         const int np = (nt + 1) >> 1;
         const unsigned nz = __ballot_sync(0xffffffffu, np > 0);
@@ -1075,20 +1079,41 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
             if (lane >= o) incl += y;
         }
         const int excl = incl - np;
-        const int total = __shfl_sync(0xffffffffu, incl, 31);
-        const int nnz = __popc(nz);
-        // the records' coil values (dcf * k) into the slots by bulk copies,
-        // slot c for the c-th record with taps: lane 0 arms the mbarrier with
-        // the batch's bytes before any copy is issued
-        if (nnz > 0) {
-            if (lane == 0) mbar_expect_tx(mbar, (unsigned)nnz * vbytes);
-            __syncwarp();
-            if (np > 0) {
-                const int c = __popc(nz & ((1u << lane) - 1u));
-                table4[c] = make_int4((int)(unsigned)rw, (int)(((rw >> 32) & 0xFF) | ((unsigned)nt << 8)), excl, 0);
-                bulk_copy_g2s(stage + ((unsigned)c << 7), kt + (IT)(unsigned)rw * vstride, vbytes, mbar);
+        const int all = __shfl_sync(0xffffffffu, incl, 31);
+        // pairs this window processes, records it finishes (a prefix: incl
+        // grows with the lane) and records it stages (those with pairs below
+        // `total`, also a prefix of the records with taps)
+        const int total = wbase + kLaneBatch >= nrec ? all : min(all, 32 * max(all >> 5, 1));
+        const int consumed = __popc(__ballot_sync(0xffffffffu, incl <= total));
+        const unsigned staged = __ballot_sync(0xffffffffu, np > 0 && excl < total);
+        const int nnz = __popc(staged);
+        {
+            // the next window: records consumed + lane of (this window, the next 32)
+            const int src = consumed + lane;
+            const unsigned long long a = __shfl_sync(0xffffffffu, rw, src & 31);
+            const unsigned long long b = __shfl_sync(0xffffffffu, rw_next, src & 31);
+            const int done = total - __shfl_sync(0xffffffffu, excl, consumed & 31);
+            unsigned long long nrw = src < kLaneBatch ? a : b;
+            if (lane == 0 && consumed < kLaneBatch && done > 0)  // 2 done taps per done pair
+                nrw = nrw + ((unsigned long long)(2 * done) << 32) - ((unsigned long long)(2 * done) << 40);
+            const unsigned long long nnext = load_rw(wbase + consumed + kLaneBatch);
+            // the staged records' coil values (dcf * k) into the slots by bulk
+            // copies, slot c for the c-th: lane 0 arms the mbarrier with the
+            // window's bytes before any copy is issued
+            if (nnz > 0) {
+                if (lane == 0) mbar_expect_tx(mbar, (unsigned)nnz * vbytes);
+                __syncwarp();
+                if ((staged >> lane) & 1u) {
+                    const int c = __popc(staged & ((1u << lane) - 1u));
+                    table4[c] =
+                        make_int4((int)(unsigned)rw, (int)(((rw >> 32) & 0xFF) | ((unsigned)nt << 8)), excl, 0);
+                    bulk_copy_g2s(stage + ((unsigned)c << 7), kt + (IT)(unsigned)rw * vstride, vbytes, mbar);
+                }
             }
+            rw = nrw;
+            rw_next = nnext;
         }
+        wbase += consumed;
         __syncwarp();
         // pass setup: the lane's pair number p0 + lane, its record (compact
         // index cr), pair offset and tap words
@@ -1147,7 +1172,7 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
                 }
             }
         }
-        __syncwarp();  // the next batch rewrites the table and the slots
+        __syncwarp();  // the next window rewrites the table and the slots
     }
     __syncthreads();
     if (it.slot < 0) {
