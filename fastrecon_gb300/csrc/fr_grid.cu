@@ -127,12 +127,6 @@ __device__ __forceinline__ int2 lds_s32x2(unsigned a)
     asm volatile("ld.shared.v2.s32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "r"(a) : "memory");
     return r;
 }
-__device__ __forceinline__ unsigned lds_u32(unsigned a)
-{
-    unsigned r;
-    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(r) : "r"(a) : "memory");
-    return r;
-}
 __device__ __forceinline__ float lds_f32(unsigned a)
 {
     float r;
