@@ -184,6 +184,9 @@ long long fr_kernel_launches(void);
  * (cuGridLut.cu:28-48,231-309; CPU oracle GridLut.cpp:80-147)
  * d_kdata: channels x n complex64; d_dcf: n floats; d_grid: channels x G^d
  * complex64, fully overwritten (cells no sample touches are written 0).
+ * The scatter's waits on its bulk copies are bounded: one that expires sets
+ * the plan's error word, and the plan's next fr_grid returns
+ * FR_ERR_DEVICE_TIMEOUT (the grid of the call that expired is not valid).
  * ---------------------------------------------------------------------- */
 int fr_grid(fr_plan plan, const float *d_kdata, const float *d_dcf, int channels,
             float *d_grid, void *stream);
