@@ -861,13 +861,14 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 
 // ---------------------------------------------------------------------------
 // Tap-lane scatter (rows of 32 coil floats, the tap lists of the plan): each
-// lane owns two taps of one bin record and adds them for all 32 coil floats
-// of its coil group, so the tap's cell row and weight stay in the lane's
-// registers and no per-record tap list goes through shared memory.
+// lane owns a group of kLaneTaps taps of one bin record and adds them for all
+// 32 coil floats of its coil group, so the taps' cell rows and weights stay
+// in the lane's registers and no per-record tap list goes through shared
+// memory.
 //
-// A warp holds 32 of its records at a time (a window): their tap pairs are
+// A warp holds 32 of its records at a time (a window): their tap groups are
 // numbered by a warp scan and dealt to the lanes 32 per pass, so a pass packs
-// the pairs of several records (a record's pairs are consecutive).  Each
+// the groups of several records (a record's groups are consecutive).  Each
 // record's 32 coil values (dcf * k) are first copied into a 128-byte slot of
 // the warp's staging area by a bulk (TMA) copy, issued by the lane holding
 // the record and completing on the warp's mbarrier; the item's fixed-point
@@ -882,10 +883,11 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 // ---------------------------------------------------------------------------
 constexpr int kLaneWarps = 8;   // 256 threads per CTA
 constexpr int kLaneBatch = 32;  // records per warp window (one per lane)
+constexpr int kLaneTaps = 4;    // taps of one record per lane (one read of its values serves them all)
 
 // Shared-memory layout of grid_lanes_kernel from its 128-byte aligned base:
 // tile [K][32] int32 | weights [L] | per warp: value slots [32][32] floats,
-// record table [32] int4 {sample, first word | taps << 8, first pair, 0} |
+// record table [32] int4 {sample, first word | taps << 8, first group, 0} |
 // per warp one mbarrier (8 bytes).
 struct LaneSmem {
     unsigned lutw, stage, table, mbar, end;
@@ -1056,15 +1058,16 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
         return k < nrec ? __ldg(trecs + (size_t)kLaneWarps * k) : 0ull;
     };
     // Records go through a window of 32, one per lane.  A window processes
-    // only whole passes of 32 tap pairs (the warp's last window: all its
-    // pairs); the records it finished leave, the rest (the first possibly
+    // only whole passes of 32 tap groups (the warp's last window: all its
+    // groups); the records it finished leave, the rest (the first possibly
     // part-done: its first tap word and tap count advanced past the done
-    // pairs) move to the front and the window fills up from the next records.
+    // groups) move to the front and the window fills up from the next records.
     unsigned long long rw = load_rw(0), rw_next = load_rw(kLaneBatch);
     for (int wbase = 0; wbase < nrec;) {
-        // this lane's record of the window: its tap pairs, their first number
+        // this lane's record of the window: its tap groups (kLaneTaps taps
+        // each, the last possibly short), their first number
         const int nt = (int)((rw >> 40) & 0xFF);
-        const int np = (nt + 1) >> 1;
+        const int np = (nt + kLaneTaps - 1) / kLaneTaps;
         const unsigned nz = __ballot_sync(0xffffffffu, np > 0);
         int incl = np;
 #pragma unroll
@@ -1074,8 +1077,8 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
         }
         const int excl = incl - np;
         const int all = __shfl_sync(0xffffffffu, incl, 31);
-        // pairs this window processes, records it finishes (a prefix: incl
-        // grows with the lane) and records it stages (those with pairs below
+        // groups this window processes, records it finishes (a prefix: incl
+        // grows with the lane) and records it stages (those with groups below
         // `total`, also a prefix of the records with taps)
         const int total = wbase + kLaneBatch >= nrec ? all : min(all, 32 * max(all >> 5, 1));
         const int consumed = __popc(__ballot_sync(0xffffffffu, incl <= total));
@@ -1088,8 +1091,10 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
             const unsigned long long b = __shfl_sync(0xffffffffu, rw_next, src & 31);
             const int done = total - __shfl_sync(0xffffffffu, excl, consumed & 31);
             unsigned long long nrw = src < kLaneBatch ? a : b;
-            if (lane == 0 && consumed < kLaneBatch && done > 0)  // 2 done taps per done pair
-                nrw = nrw + ((unsigned long long)(2 * done) << 32) - ((unsigned long long)(2 * done) << 40);
+            if (lane == 0 && consumed < kLaneBatch && done > 0) {  // kLaneTaps done taps per done group
+                const unsigned long long dt = (unsigned long long)(kLaneTaps * done);
+                nrw = nrw + (dt << 32) - (dt << 40);
+            }
             const unsigned long long nnext = load_rw(wbase + consumed + kLaneBatch);
             // the staged records' coil values (dcf * k) into the slots by bulk
             // copies, slot c for the c-th: lane 0 arms the mbarrier with the
@@ -1109,30 +1114,31 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
         }
         wbase += consumed;
         __syncwarp();
-        // pass setup: the lane's pair number p0 + lane, its record (compact
-        // index cr), pair offset and tap words
+        // pass setup: the lane's group number p0 + lane, its record (compact
+        // index cr), the taps left in the group (nl) and their tap words
         int recbase = 0;
-        auto pass_setup = [&](int p0, int &cr, int &pi, int &ntr, unsigned &t0, unsigned &t1) {
-            // bit i of starts: a record's first pair is pair p0 + i
+        auto pass_setup = [&](int p0, int &cr, int &nl, unsigned *tg) {
+            // bit i of starts: a record's first group is group p0 + i
             const bool in_pass = np > 0 && excl >= p0 && excl < p0 + 32;
             const unsigned starts = __reduce_or_sync(0xffffffffu, in_pass ? 1u << (excl - p0) : 0u);
             cr = recbase + __popc(starts & (0xffffffffu >> (31 - lane))) - 1;
             recbase += __popc(starts);
-            pi = 0;
-            ntr = 0;
-            t0 = t1 = 0u;
+            nl = 0;
+#pragma unroll
+            for (int k = 0; k < kLaneTaps; ++k) tg[k] = 0u;
             if (p0 + lane < total) {
                 const int4 e = table4[cr];
-                ntr = e.y >> 8;
-                pi = 2 * (p0 + lane - e.z);
-                const IT tb = (IT)(unsigned)e.x * tw + (IT)(e.y & 0xFF) + (IT)pi;
-                t0 = __ldg(taps + tb);
-                if (pi + 1 < ntr) t1 = __ldg(taps + tb + 1);
+                const int gi = kLaneTaps * (p0 + lane - e.z);
+                nl = min((e.y >> 8) - gi, kLaneTaps);
+                const IT tb = (IT)(unsigned)e.x * tw + (IT)(e.y & 0xFF) + (IT)gi;
+#pragma unroll
+                for (int k = 0; k < kLaneTaps; ++k)
+                    if (k < nl) tg[k] = __ldg(taps + tb + k);
             }
         };
-        int cr_n, pi_n, ntr_n;
-        unsigned t0_n, t1_n;
-        pass_setup(0, cr_n, pi_n, ntr_n, t0_n, t1_n);  // the first pass's tap words load during the copies
+        int cr_n, nl_n;
+        unsigned t_n[kLaneTaps];
+        pass_setup(0, cr_n, nl_n, t_n);  // the first pass's tap words load during the copies
         if (nnz > 0) {
             if (!mbar_wait(mbar, parity)) {
                 // a copy that never lands: report it and wait once more for
@@ -1143,26 +1149,32 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
             parity ^= 1u;
         }
         for (int p0 = 0; p0 < total; p0 += 32) {
-            const int cr = cr_n, pi = pi_n, ntr = ntr_n;
-            const unsigned t0 = t0_n, t1 = t1_n;
-            if (p0 + 32 < total) pass_setup(p0 + 32, cr_n, pi_n, ntr_n, t0_n, t1_n);
+            const int cr = cr_n, nl = nl_n;
+            unsigned t[kLaneTaps];
+#pragma unroll
+            for (int k = 0; k < kLaneTaps; ++k) t[k] = t_n[k];
+            if (p0 + 32 < total) pass_setup(p0 + 32, cr_n, nl_n, t_n);
             if (p0 + lane < total) {
-                const bool has1 = pi + 1 < ntr;
-                const unsigned c0 = min(t0 & cmask, (unsigned)(K - 1)), c1 = min(t1 & cmask, (unsigned)(K - 1));
-                // the item's power-of-two scale on the weights (exact: the
-                // same products w * v * S as scaling the values)
-                const float w0 = __fmul_rn(lutw_s[min(t0 >> kTapCellBits, (unsigned)(P.L - 1))], sc);
-                const float w1 = has1 ? __fmul_rn(lutw_s[min(t1 >> kTapCellBits, (unsigned)(P.L - 1))], sc) : 0.f;
-                const unsigned a0 = (acc + (c0 << 7)) | lane4, a1 = (acc + (c1 << 7)) | lane4;
+                // each tap's cell row (this lane's float offset folded in)
+                // and weight, the item's power-of-two scale on the weight
+                // (exact: the same products w * v * S as scaling the values)
+                unsigned a[kLaneTaps];
+                float w[kLaneTaps];
+#pragma unroll
+                for (int k = 0; k < kLaneTaps; ++k) {
+                    a[k] = (acc + (min(t[k] & cmask, (unsigned)(K - 1)) << 7)) | lane4;
+                    w[k] = k < nl ? __fmul_rn(lutw_s[min(t[k] >> kTapCellBits, (unsigned)(P.L - 1))], sc) : 0.f;
+                }
                 const unsigned va = (stage + ((unsigned)cr << 7)) | lane4;
                 float v[32];
 #pragma unroll
                 for (int f = 0; f < 32; ++f) v[f] = lds_f32_v(va ^ ((unsigned)f << 2));
 #pragma unroll
-                for (int f = 0; f < 32; ++f) red_add_fx(a0 ^ ((unsigned)f << 2), w0, v[f]);
-                if (has1) {
+                for (int k = 0; k < kLaneTaps; ++k) {
+                    if (k < nl) {
 #pragma unroll
-                    for (int f = 0; f < 32; ++f) red_add_fx(a1 ^ ((unsigned)f << 2), w1, v[f]);
+                        for (int f = 0; f < 32; ++f) red_add_fx(a[k] ^ ((unsigned)f << 2), w[k], v[f]);
+                    }
                 }
             }
         }
