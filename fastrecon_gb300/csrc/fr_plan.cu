@@ -456,12 +456,13 @@ __device__ __forceinline__ void sample_taps(const BinGeom &g, const TapGeom &tg,
     }
 }
 
-// The same walk for samples whose range touches at most 8 tiles, with the
-// per-record tap counts and first words packed as bytes in two 64-bit
-// registers (byte j: record j) instead of shared-memory counters: no
-// load-add-store chain through shared memory per candidate cell, and the LUT
-// thresholds read from shared memory.  The words and their order are those
-// of sample_taps.
+// The same walk for samples whose range touches at most 8 tiles (at most 2
+// along x), with the per-record tap counts and first words packed as bytes
+// in two 64-bit registers (byte j: record j) instead of shared-memory
+// counters: no load-add-store chain through shared memory per candidate
+// cell, the counting walk one bitmask of valid x candidates per row (a popc
+// per x tile), and the LUT thresholds read from shared memory.  The words and
+// their order are those of sample_taps.
 template <int XR>
 __device__ __forceinline__ void sample_taps_pk(const BinGeom &g, const TapGeom &tg, const float *thr, const float *c,
                                                const int *s, const int *e, const TileWalk &w, bool place,
@@ -469,6 +470,7 @@ __device__ __forceinline__ void sample_taps_pk(const BinGeom &g, const TapGeom &
 {
     float dx2[XR];
     int jx[XR], lx[XR];
+    unsigned pm1 = 0u;  // candidates in the second x tile (at most 2 x tiles)
 #pragma unroll
     for (int i = 0; i < XR; ++i) {
         const int x = s[0] + i;
@@ -476,6 +478,7 @@ __device__ __forceinline__ void sample_taps_pk(const BinGeom &g, const TapGeom &
         dx2[i] = x <= e[0] ? __fmul_rn(dx, dx) : __int_as_float(0x7f800000);
         jx[i] = tile_div(g, x, 0) - w.lo[0];
         lx[i] = x - (w.lo[0] + jx[i]) * g.tile[0];
+        if (jx[i] != 0) pm1 |= 1u << i;
     }
     float fz = (float)s[2];
     for (int z = s[2]; z <= e[2]; ++z, fz = __fadd_rn(fz, 1.f)) {
@@ -491,6 +494,17 @@ __device__ __forceinline__ void sample_taps_pk(const BinGeom &g, const TapGeom &
             const int ly = y - (w.lo[1] + jy) * g.tile[1];
             const int jzy = (jz * w.n[1] + jy) * w.n[0];
             const int rowzy = (lz * g.tile[1] + ly) * g.tile[0];
+            if (!place) {
+                // counting: the row's valid candidates as a bitmask, one
+                // count per x tile (records (jz, jy, 0) and (jz, jy, 1))
+                unsigned m = 0u;
+#pragma unroll
+                for (int i = 0; i < XR; ++i)
+                    if (__fadd_rn(dzy, dx2[i]) < tg.smax) m |= 1u << i;
+                cnt += (unsigned long long)((unsigned)__popc(m & ~pm1) | ((unsigned)__popc(m & pm1) << 8))
+                       << (8u * (unsigned)jzy);
+                continue;
+            }
 #pragma unroll
             for (int i = 0; i < XR; ++i) {
                 const float s2 = __fadd_rn(dzy, dx2[i]);
@@ -1160,9 +1174,9 @@ int plan_run(fr_plan p, const float *d_traj, size_t n, cudaStream_t s)
         tg.recmax = recmax;
         // slot staging plus 2 bytes per possible record: 4 CTAs of 256 per SM
         // for the 3D 4-wide kernel (42 words, 8 records)
-        // (packed-counter form when a sample touches at most 8 tiles: slot
-        // staging plus the L thresholds)
-        const bool pk = recmax <= 8;
+        // (packed-counter form when a sample touches at most 8 tiles and at
+        // most 2 along x: slot staging plus the L thresholds)
+        const bool pk = recmax <= 8 && ((int)std::floor(2.0 * p->hw) + p->tile[0] - 1) / p->tile[0] + 1 <= 2;
         const size_t smem = pk ? (size_t)kFillThreads * (size_t)(p->tap_words | 1) * 4 + (size_t)p->L * 4
                                : (size_t)kFillThreads * ((size_t)(p->tap_words | 1) * 4 + 2 * recmax);
         // cells of a sample's range along x: at most floor(2 hw) + 1
