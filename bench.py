@@ -263,7 +263,8 @@ class RefRecon:
 def fp64_errors(w, traj, dcf, kd, torch):
     """GPU grid (fr_grid, default tiling and work items) vs the oracle's FP64
     gridding and its FP32 restatement of the reference, on the first 2 coils
-    of the workload and on the whole 2D radial configuration."""
+    of the workload (in the workload's coil group: the benchmark's scatter
+    kernel) and on the whole 2D radial configuration."""
     import numpy as np
 
     import fastrecon_gb300 as fr
@@ -276,6 +277,11 @@ def fp64_errors(w, traj, dcf, kd, torch):
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
     out = {}
+    # the workload's 2 coils in the coil group the recon uses for all of its
+    # coils, so that they go through the same scatter kernel as the benchmark
+    cg = 4
+    while cg < w["coils"] and cg < 16:
+        cg *= 2
     cases = [(w, traj, dcf, kd[:2], f"{w['desc'].split(':')[0]}, 2 of {w['coils']} coils")]
     if w is not WORKLOADS["radial2d"]:
         r2 = WORKLOADS["radial2d"]
@@ -284,7 +290,7 @@ def fp64_errors(w, traj, dcf, kd, torch):
     for wk, t, d, k, name in cases:
         G = fr.grid_size(wk["recon"], wk["os"])
         lut = o.kb_lut(wk["width"], wk["os"], wk["lut"])
-        plan = fr.GridPlan(wk["dim"], G, wk["width"], lut=lut)
+        plan = fr.GridPlan(wk["dim"], G, wk["width"], lut=lut, coil_group=cg if wk is w else 0)
         plan.set_trajectory(t)
         g = plan.grid(k.contiguous(), d).cpu().numpy()
         del plan

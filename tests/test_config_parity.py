@@ -10,7 +10,8 @@ oracle on the same seeded inputs:
   samples), |k|^2 DCF, os 1.5 (384^3 grid), 256^3 SoS, with 2 of the 16
   coils (the oracle's time grows with the coils; the trajectory, the tile
   densities and the work items -- 4,096-record items, ~75 per centre tile --
-  are those of the full configuration);
+  are those of the full configuration); and the same 2 coils in a coil
+  group of 16, through the benchmark's tap-lane scatter;
 * config 3: three frames (the sparsest, the densest and one between) of the
   64-frame dynamic spiral batch, gridded by the persistent batch kernel with
   the autotuner's tiling, 12 coils, 384^2 grid;
@@ -93,6 +94,46 @@ def test_config2_kooshball_full_trajectory(torch, oracle):
     assert traj.shape[0] == 50000 * 256
     _grid_and_image(torch, oracle, "config 2 (3D kooshball 50,000x256, 2 of 16 coils, 384^3)", traj, dcf, kd, 3,
                     256, 1.5)
+
+
+def test_config2_kooshball_full_trajectory_tap_lanes(torch, oracle):
+    """Config 2's full trajectory through the benchmark's scatter kernel: a
+    coil group of 16 (rows of 32 coil floats: the tap-lane scatter, here with
+    2 of its 16 coils filled), the full trajectory's tile densities and split
+    tiles.  Bit-equal to the per-warp tap-list scatter on the same
+    deterministic plan, and the reference's FP32 algorithm at 1e-5."""
+    import os
+
+    import fastrecon_gb300 as fr
+    from fastrecon_gb300 import synth
+    cfg = dict(synth.CONFIGS["kooshball3d"])
+    cfg["coils"] = 2
+    traj, dcf, kd = synth.make_case(**cfg, xp=torch, device="cuda")
+    G, W = fr.grid_size(256, 1.5), 4.0
+    lut = oracle.kb_lut(W, 1.5, 512)
+    td, dd = torch.from_numpy(traj).cuda(), torch.from_numpy(dcf).cuda()
+    grids = []
+    for warp_lists in (False, True):
+        if warp_lists:
+            os.environ["FR_SCATTER_WARP_LISTS"] = "1"
+        try:
+            plan = fr.GridPlan(3, G, W, lut=lut, coil_group=16, deterministic=True)
+            plan.set_trajectory(td)
+            assert plan.tap_words() > 0 and plan.stats()["slots"] > 0
+            grids.append(plan.grid(kd, dd).cpu().numpy())
+            del plan
+        finally:
+            os.environ.pop("FR_SCATTER_WARP_LISTS", None)
+    assert np.array_equal(grids[0].view(np.uint32), grids[1].view(np.uint32))
+    g = grids[0]
+    del grids
+    tn, _, _, _, _ = oracle.normalize_traj(traj, 3, G)
+    ref = oracle.grid_bands(tn, dcf, kd.cpu().numpy(), 3, G, W, lut)
+    e_ref = rel_l2(g, ref)
+    print(f"config 2 full trajectory, tap-lane scatter (coil group 16): = per-warp tap lists bit for bit; "
+          f"vs reference algorithm rel-L2 {e_ref:.2e}")
+    assert e_ref <= TOL
+    assert np.array_equal(g == 0, ref == 0)
 
 
 def _batch_frames(torch, oracle, name, trajs, kds, dcfs, dim, G, W, os_, check_frames, autotune):
