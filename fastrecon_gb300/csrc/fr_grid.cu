@@ -1020,12 +1020,14 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     float *lutw_s = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(smem4) + L_.lutw);
-    // the tile and the value slots start at zero (a slot's coils past the
-    // group's last are never copied)
+    // the tile starts at zero, and so do the value slots of a partial coil
+    // group (a slot's coils past the group's last are never copied)
     for (int i = threadIdx.x; i < K * 8; i += blockDim.x) smem4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 *stage_all = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.stage);
-    for (int i = threadIdx.x; i < kLaneWarps * kLaneBatch * 8; i += blockDim.x)
-        stage_all[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (min(CG, P.channels - cg * CG) < 16) {  // copies of fewer than 128 bytes (a partial group)
+        float4 *stage_all = reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(smem4) + L_.stage);
+        for (int i = threadIdx.x; i < kLaneWarps * kLaneBatch * 8; i += blockDim.x)
+            stage_all[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     for (int i = threadIdx.x; i < P.L; i += blockDim.x) lutw_s[i] = P.lutw[i];
     const float inv = P.item_inv[blockIdx.x];
     const float sc = __fdiv_rn(1.f, inv);  // exact: a power of two

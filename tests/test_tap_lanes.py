@@ -1,5 +1,5 @@
 """GPU: the tap-lane scatter (grid_lanes_kernel, the default for coil groups
-of 16: a lane owns two taps of a bin record and adds them for all 32 coil
+of 16: a lane owns 4 taps of a bin record and adds them for all 32 coil
 floats) against the per-warp tap-list scatter it replaces
 (FR_SCATTER_WARP_LISTS=1) and against the reference.  Both add the same
 fixed-point values, so with the same records in every work item
@@ -44,9 +44,9 @@ def _kspace(coils, n, seed):
     return (rng.standard_normal((coils, n)) + 1j * rng.standard_normal((coils, n))).astype(np.complex64)
 
 
-def _grid(torch, c, kd, **kw):
+def _grid(torch, c, kd, coil_group=16, **kw):
     import fastrecon_gb300 as fr
-    p = fr.GridPlan(c["dim"], c["G"], c["W"], lut=c["lut"], coil_group=16, deterministic=True, **kw)
+    p = fr.GridPlan(c["dim"], c["G"], c["W"], lut=c["lut"], coil_group=coil_group, deterministic=True, **kw)
     p.set_trajectory(torch.from_numpy(c["traj"]).cuda())
     assert p.tap_words() > 0
     g = p.grid(torch.from_numpy(np.ascontiguousarray(kd)).cuda(), torch.from_numpy(c["dcf"]).cuda())
