@@ -9,7 +9,7 @@ mean k-space energy of a synthetic object there, so that the fit is best
 where DCF errors reach the image; the target is normalised by the kernel
 mass (target_offset) so that grids of different oversampling agree.  The network is trained on Pipe-Menon weights
 computed on the GPU (``GridPlan.dcf_pipe``); those weights remain its
-fallback and the reference its images are judged against.
+fallback and the reference its images are compared with.
 
 Every step runs in libfastrecon_gb300.so: fr_density_counts,
 fr_dcf_features, fr_mlp_forward / fr_mlp_backward / fr_mlp_adam.  PyTorch
