@@ -884,6 +884,7 @@ __global__ void __launch_bounds__(512, 2) grid_taps_kernel(GridParams P)
 constexpr int kLaneWarps = 8;   // 256 threads per CTA
 constexpr int kLaneBatch = 32;  // records per warp window (one per lane)
 constexpr int kLaneTaps = 4;    // taps of one record per lane (one read of its values serves them all)
+static_assert(kLaneTaps == 4, "a lane's taps are loaded as one 16-byte word from aligned runs");
 
 // Shared-memory layout of grid_lanes_kernel from its 128-byte aligned base:
 // tile [K][32] int32 | weights [L] | per warp: value slots [32][32] floats,
@@ -1133,9 +1134,19 @@ __global__ void __launch_bounds__(kLaneWarps * 32, 2) grid_lanes_kernel(GridPara
                 const int gi = kLaneTaps * (p0 + lane - e.z);
                 nl = min((e.y >> 8) - gi, kLaneTaps);
                 const IT tb = (IT)(unsigned)e.x * tw + (IT)(e.y & 0xFF) + (IT)gi;
+                if ((tb & (IT)3) == 0) {
+                    // a run the plan placed on a 4-word boundary (slots are
+                    // multiples of 4 words, so the group stays in the slot)
+                    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(taps + tb));
+                    tg[0] = q.x;
+                    tg[1] = q.y;
+                    tg[2] = q.z;
+                    tg[3] = q.w;
+                } else {
 #pragma unroll
-                for (int k = 0; k < kLaneTaps; ++k)
-                    if (k < nl) tg[k] = __ldg(taps + tb + k);
+                    for (int k = 0; k < kLaneTaps; ++k)
+                        if (k < nl) tg[k] = __ldg(taps + tb + k);
+                }
             }
         };
         int cr_n, nl_n;

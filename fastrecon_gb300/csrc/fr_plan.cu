@@ -683,12 +683,20 @@ __global__ void __launch_bounds__(kFillThreads) fill_taps_pk_kernel(const float4
             else
                 sample_taps_pk<XR>(g, tg, thr, c, s, e, w, false, cnt, 0ull, mine);
         }
-        int tot = 0;
+        // runs at multiples of 4 words when the sample's padded runs fit in
+        // its slot (the scatter then loads a lane's 4 taps as one 16-byte
+        // word), else packed
+        int tot = 0, totp = 0;
+        unsigned long long offp = 0ull;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
+            const int cj = (int)((cnt >> (8 * j)) & 255ull);
             off |= (unsigned long long)min(tot, 255) << (8 * j);
-            tot += (int)((cnt >> (8 * j)) & 255ull);
+            offp |= (unsigned long long)min(totp, 255) << (8 * j);
+            tot += cj;
+            totp += (cj + 3) & ~3;
         }
+        if (totp <= tg.words) off = offp;
         if (tot <= tg.words && cnt_t > 0) {
             unsigned long long k = 0ull;  // taps placed per record
             if (narrow)
@@ -1304,7 +1312,9 @@ void tap_slot_layout(int dim, float hw, int *words)
                         }
                 nmax = std::max(nmax, cnt);
             }
-    *words = nmax;
+    // a multiple of 4 words: slots start on 16-byte boundaries, so runs placed
+    // at multiples of 4 words in a slot are 16-byte aligned
+    *words = (nmax + 3) & ~3;
 }
 
 int plan_chunk(size_t n, int dim)
